@@ -1,0 +1,412 @@
+"""Benchmark: Lindblad RK4 instance-steps/s on one GB300.
+
+Default workload ``exciton4096``: 4096 Frenkel-exciton aggregates with
+N = n + 1, n ~ U{8..64}, pure dephasing (diagonal collapse operators),
+rho(0) = mu rho_g, dt = 0.05, 4000 RK4 steps, output C(t) = Tr[mu rho(t)]
+for every instance and step (the reference's ``correlation_2op_1t``,
+``pyqed/oqs.py:717-791``, over a batch).  One bench step = one full
+propagation of the batch (4096 x 4000 instance-steps).
+
+  python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload exciton4096|driven256|jc16] [--n-inst N] [--nt T]
+
+Prints one JSON line.  ``value`` is the chosen path with inputs resident in
+HBM (device-timed with CUDA events on the launch stream, L2 flushed between
+steps); ``e2e`` times the public batched API including the host->device copy
+of every input from pinned memory and the device->host read of C(t).
+``plain`` is the FP32 CUDA-core path on the same inputs; ``cpu_baseline`` is
+the oracle port of the reference's dense algorithm on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Lindblad RK4 instance-steps/s: chosen vs plain on GB300 at |drho|<=1e-5; bwd/fwd"
+UNIT = "instance-steps/s"
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def make_workload(name, n_inst=None, nt=None):
+    from pyqed_gb300 import workloads as W
+    from pyqed_gb300.batch import prepare_batch
+    if name == "exciton4096":
+        n_inst = n_inst or 4096
+        ex = W.exciton_batch(n_inst=n_inst)
+        nt = nt or ex["nt"]
+        cops = [[np.diag(c) for c in cd] for cd in ex["c_diag"]]
+        seeds = [m @ r for m, r in zip(ex["mu"], ex["rho_g"])]
+        bi = prepare_batch(ex["H"], cops, seeds, [[m] for m in ex["mu"]])
+        desc = dict(workload=name, n_inst=n_inst, nt=nt, dt=ex["dt"],
+                    N_range=[int(bi.dims.min()), int(bi.dims.max())],
+                    collapse_ops="diagonal (n dephasing projectors)",
+                    output="C(t)=Tr[mu rho(t)], (n_inst, nt) complex")
+        flops = int(64 * np.sum(bi.dims.astype(np.int64) ** 3))
+        return dict(bi=bi, nt=nt, dt=ex["dt"], obs_t0=False, drive=None, desc=desc,
+                    flops_per_step=flops, ex=ex)
+    if name == "driven256":
+        n_inst = n_inst or 256
+        d = W.driven_batch(n_inst=n_inst, nt=nt or 2000)
+        nt = d["nt"]
+        cops = [[np.sqrt(d["gamma"][b][k]) * d["L"][b][k] for k in range(2)] for b in range(n_inst)]
+        bi = prepare_batch(d["H0"], cops, d["rho0"], [[o] for o in d["O"]],
+                           drive_ops=[[m] for m in d["mu"]])
+        desc = dict(workload=name, n_inst=n_inst, nt=nt, dt=d["dt"], N=64, K=2,
+                    drive="H(t)=H0-E(t)mu, shared GP pulse")
+        flops = int(64 * 3 * np.sum(bi.dims.astype(np.int64) ** 3))
+        return dict(bi=bi, nt=nt, dt=d["dt"], obs_t0=False, drive=d["E"][None, :].copy(),
+                    desc=desc, flops_per_step=flops)
+    if name == "jc16":
+        jc = W.jaynes_cummings()
+        nt = nt or jc["nt"]
+        bi = prepare_batch([jc["H"]], [jc["c_ops"]], [jc["rho0"]], [jc["e_ops"]])
+        desc = dict(workload=name, n_inst=1, nt=nt, dt=jc["dt"], N=16, K=2)
+        return dict(bi=bi, nt=nt, dt=jc["dt"], obs_t0=True, drive=None, desc=desc,
+                    flops_per_step=int(64 * 3 * 16 ** 3))
+    raise SystemExit("unknown workload %s" % name)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=["nvidia-smi unavailable"])
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return dict(sm_mhz=float(np.median(sm)) if sm else None, sm_max_mhz=smax,
+                    samples=len(sm), reasons=sorted(reasons))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    from pyqed_gb300.build import build
+    from pyqed_gb300.engine import Propagator
+    build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    wl = make_workload(args.workload, args.n_inst, args.nt)
+    bi, nt, dt = wl["bi"], wl["nt"], wl["dt"]
+    n_inst = int(bi.dims.size)
+    chosen = args.precision
+    paths = [chosen] + ([] if args.no_plain or chosen == "fp32" else ["fp32"])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    drive_shared = wl["drive"] is None or wl["drive"].ndim == 2
+
+    def new_prop(prec):
+        return Propagator(bi.dims, nt=nt, dt=dt, n_cops=bi.n_cops, cops_kind=bi.cops_kind,
+                          n_eops=bi.n_eops, n_drive=bi.n_drive, obs_t0=wl["obs_t0"],
+                          precision=prec, drive_shared=drive_shared, device=dev)
+
+    results = {}
+    rho0_dev = None
+    drive_dev = torch.from_numpy(wl["drive"].ravel()).to(dev) if wl["drive"] is not None else None
+    for prec in paths:
+        prop = new_prop(prec)
+        prop.set_operators(bi.H, bi.cops, bi.eops, bi.dops)
+        rho0_dev = prop.to_device(bi.rho0)
+        out = prop.alloc_outputs(want_obs=True, want_rho=False)
+        stream = torch.cuda.current_stream(dev)
+        for _ in range(args.warmup):
+            prop.propagate_device(rho0_dev, drive_dev, out)
+        torch.cuda.synchronize()
+        prop.check_errors()
+        clocks = ClockSampler(0)
+        if prec == chosen:
+            clocks.start()
+        times = []
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)  # evict L2 between timed steps (untimed)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            prop.propagate_device(rho0_dev, drive_dev, out)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        wall = time.perf_counter() - t_wall0
+        clk = clocks.stop() if prec == chosen else None
+        prop.check_errors()
+        info = prop.info()
+        t = float(np.mean(times))
+        results[prec] = dict(sec_per_step=t, times=times, wall=wall, info=info, clocks=clk,
+                             obs=prop.unpack_obs(out[0]) if out[0] is not None else None)
+        prop.close()
+
+    # ---- end to end through the public batched API (host buffers) ---------------
+    prop = new_prop(chosen)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory() if a is not None else None  # noqa: E731
+    host = [pin(x) for x in (bi.H, bi.cops, bi.eops, bi.dops, bi.rho0)]
+    host_drive = pin(wl["drive"].ravel()) if wl["drive"] is not None else None
+    out = prop.alloc_outputs(want_obs=True, want_rho=False)
+    obs_host = torch.empty(out[0].numel(), dtype=torch.complex128).pin_memory()
+    h2d = sum(x.numel() * x.element_size() for x in host if x is not None)
+    h2d += host_drive.numel() * 8 if host_drive is not None else 0
+    d2h = obs_host.numel() * obs_host.element_size()
+    stream = torch.cuda.current_stream(dev)
+
+    def e2e_step():
+        dv = [x.to(dev, non_blocking=True) if x is not None else None for x in host]
+        drv = host_drive.to(dev, non_blocking=True) if host_drive is not None else None
+        prop.set_operators(dv[0], dv[1], dv[2], dv[3])
+        prop.propagate_device(dv[4], drv, out)
+        obs_host.copy_(out[0], non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_times.append(e0.elapsed_time(e1) / 1e3)
+    prop.check_errors()
+    prop.close()
+    e2e_t = float(np.mean(e2e_times))
+
+    inst_steps = n_inst * nt
+    ch = results[chosen]
+    flops_launch = wl["flops_per_step"] * nt
+    achieved = flops_launch / ch["sec_per_step"] / 1e12
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    line = dict(
+        metric=METRIC, value=inst_steps / ch["sec_per_step"], unit=UNIT, n_gpus=1,
+        steps=args.steps, warmup=args.warmup, ms_per_step=ch["sec_per_step"] * 1e3,
+        higher_is_better=True, scaling="weak", vs_baseline=None,
+        dtype={"fp32": "c64 (fp32)", "fp64": "c128 (fp64)", "3xtf32": "c64 via 3xTF32",
+               "3xbf16": "c64 via 3xBF16"}[chosen],
+        data="synthetic (seeded generators, pyqed_gb300/workloads.py)",
+        config=dict(wl["desc"], path=chosen, schedule=ch["info"]["schedule"],
+                    l2="flushed between timed steps (256 MB write)"),
+        gpu_launches=args.steps * ch["info"]["launches"],
+    )
+    # roofline of the dominant kernel (the propagate launch)
+    if chosen in ("3xtf32", "3xbf16"):
+        pk = peaks.get("bf16_tflops", 1900.0)
+        if chosen == "3xtf32":
+            pk = pk / 2.0
+        line["roofline"] = dict(bound="tensor", achieved=achieved, peak=pk, unit="TFLOP/s",
+                                frac=achieved / pk, traffic=None,
+                                note="algorithmic 64*N^3 flops per instance-step; peak = "
+                                     + ("measured bf16 / 2 (TF32 rate)" if chosen == "3xtf32"
+                                        else "measured bf16"))
+    else:
+        clk_mhz = (ch["clocks"] or {}).get("sm_max_mhz") or 2070.0
+        pk = 152 * 128 * 2 * clk_mhz * 1e6 / 1e12
+        line["roofline"] = dict(bound="fp32", achieved=achieved, peak=pk, unit="TFLOP/s",
+                                frac=achieved / pk, traffic=None,
+                                note="FP32 CUDA-core path; peak = 152 SMs x 128 FMA x 2 x max SM "
+                                     "clock (nominal, no measured FP32 peak available)")
+    line["plain"] = None
+    if "fp32" in results and chosen != "fp32":
+        pl = results["fp32"]
+        line["plain"] = dict(value=inst_steps / pl["sec_per_step"], ms_per_step=pl["sec_per_step"] * 1e3,
+                             speedup_chosen_over_plain=pl["sec_per_step"] / ch["sec_per_step"])
+    line["e2e"] = dict(value=inst_steps / e2e_t, unit=UNIT, ms_per_step=e2e_t * 1e3,
+                       h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
+                       api="pyqed_gb300.engine.Propagator.set_operators + propagate "
+                           "(C ABI lgb_plan_set_operators/lgb_plan_propagate)")
+    line["clocks"] = ch["clocks"]
+    # CPU baseline (oracle port of the reference's dense algorithm) and accuracy
+    if not args.no_cpu:
+        line["cpu_baseline"], line["accuracy"] = cpu_baseline_and_accuracy(
+            wl, results, args, chosen)
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline / reference arm (the oracle port; the only oracle use here)
+# ---------------------------------------------------------------------------
+def _sample_indices(dims, count):
+    order = np.argsort(dims, kind="stable")
+    q = ((np.arange(count) + 0.5) / count * len(dims)).astype(int)
+    return sorted(int(order[i]) for i in q)
+
+
+def cpu_port_rate(wl, n_sample, steps):
+    """Reference algorithm (dense RHS, pyqed/oqs.py:697-715 + pyqed/phys.py:1051-1064),
+    restated by the oracle, on a stratified sample of instances."""
+    from oracle import lindblad_oracle as O
+    bi = wl["bi"]
+    dims = bi.dims
+    idx = _sample_indices(dims, min(n_sample, len(dims)))
+    off = np.concatenate([[0], np.cumsum(dims.astype(np.int64) ** 2)])
+    doff = np.concatenate([[0], np.cumsum(dims.astype(np.int64))])
+    K = bi.n_cops
+    tot = 0.0
+    for b in idx:
+        N = int(dims[b])
+        H = bi.H[off[b]:off[b + 1]].reshape(N, N)
+        if bi.cops_kind == "diag":
+            cd = bi.cops[K * doff[b]: K * doff[b + 1]].reshape(K, N)
+            cops = [np.diag(c) for c in cd]
+        elif bi.cops_kind == "dense":
+            cops = list(bi.cops[K * off[b]: K * off[b + 1]].reshape(K, N, N))
+        else:
+            cops = []
+        rho = bi.rho0[off[b]:off[b + 1]].reshape(N, N).copy()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            rho = O.rk4_step(rho, wl["dt"], H, cops)
+        tot += time.perf_counter() - t0
+    # mean time per instance-step over a sample stratified by N = the
+    # workload's mean; rate over the whole batch follows
+    mean_t = tot / (len(idx) * steps)
+    return 1.0 / mean_t, idx
+
+
+def cpu_baseline_and_accuracy(wl, results, args, chosen):
+    import multiprocessing
+    cores = os.cpu_count() or 1
+    rate, idx = cpu_port_rate(wl, args.cpu_sample, args.cpu_steps)
+    cb = dict(value=rate, unit=UNIT, cores=cores, kind="port",
+              sample="%d instances stratified by N x %d RK4 steps, dense numpy complex128 "
+                     "(oracle restatement of the reference's RHS + rk4, BLAS threads = host)"
+                     % (len(idx), args.cpu_steps))
+    acc = None
+    if wl.get("ex") is not None and args.workload == "exciton4096":
+        from oracle import lindblad_oracle as O
+        ex = wl["ex"]
+        pick = _sample_indices(wl["bi"].dims, args.acc_sample)
+        acc = {}
+        refs = {b: O.propagate_diag_correlation(ex["H"][b], ex["mu"][b], ex["rho_g"][b],
+                                                ex["c_diag"][b], ex["dt"], wl["nt"]) for b in pick}
+        for prec, r in results.items():
+            errs = [np.abs(r["obs"][b, :, 0] - refs[b]).max() / np.abs(refs[b]).max() for b in pick]
+            acc[prec] = dict(max_rel_err_C=float(max(errs)), instances=pick, nt=wl["nt"])
+    del multiprocessing
+    return cb, acc
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU algorithm (oracle port) on the
+    host cores; one step = a bounded stratified sample of the workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = make_workload(args.workload, args.n_inst, args.nt)
+    for _ in range(args.warmup):
+        cpu_port_rate(wl, max(2, args.cpu_sample // 4), 1)
+    rates = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, idx = cpu_port_rate(wl, args.cpu_sample, args.cpu_steps)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    v = float(np.mean(rates))
+    cores = os.cpu_count() or 1
+    sample = ("%d instances stratified by N x %d RK4 steps per bench step, dense numpy complex128 "
+              "restatement of the reference's RHS + rk4" % (len(idx), args.cpu_steps))
+    line = dict(metric=METRIC, value=v, unit=UNIT, n_gpus=args.gpus, steps=args.steps,
+                warmup=args.warmup, ms_per_step=wall / max(1, args.steps) * 1e3,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="c128 (fp64)",
+                data="synthetic (seeded generators, pyqed_gb300/workloads.py)",
+                config=dict(make_workload_desc(wl), path="reference CPU (oracle port)"),
+                impl="reference",
+                cpu_baseline=dict(value=v, unit=UNIT, cores=cores, kind="port", sample=sample),
+                e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                gpu_launches=0)
+    print(json.dumps(line))
+
+
+def make_workload_desc(wl):
+    return dict(wl["desc"])
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="exciton4096")
+    ap.add_argument("--precision", default=os.environ.get("LGB_BENCH_PRECISION", "fp32"))
+    ap.add_argument("--n-inst", type=int, default=None)
+    ap.add_argument("--nt", type=int, default=None)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=16)
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--acc-sample", type=int, default=4)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        # independent replicas of the batch, one per GPU (instances shard with
+        # no exchange); rank 0 reports.  Not exercised on this single-GPU pool.
+        raise SystemExit("multi-GPU runs are not supported by this build")
+    run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

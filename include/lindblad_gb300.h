@@ -1,0 +1,153 @@
+/*
+ * lindblad_gb300.h -- C ABI of the GB300-native Lindblad RK4 propagator.
+ *
+ * The reference (binggu56/pyqed, pure Python) has no native interface: its
+ * Lindblad path is the Python class pyqed.oqs.LindbladSolver
+ * (pyqed/oqs.py:1114-1330).  Each entry point below replaces one piece of
+ * that class's call stack; the Python mirror pyqed_gb300.oqs.LindbladSolver
+ * binds them with ctypes exactly as a maintainer of the reference would
+ * (INTEGRATION.md shows the binding).
+ *
+ * Conventions
+ *  - All matrices are complex128, interleaved (re, im) doubles, row-major.
+ *  - A batch holds n_inst independent instances of dimensions dims[b].
+ *    Instance b's N x N operators start at complex offset off[b] =
+ *    sum_{a<b} dims[a]^2 ("packed layout").  Per-instance families use
+ *    count * off[b] + k * dims[b]^2 (collapse operators, observables,
+ *    drive operators, stored states); diagonal collapse operators use
+ *    n_cops * doff[b] + k * dims[b] with doff[b] = sum_{a<b} dims[a].
+ *  - Every pointer passed to lgb_plan_set_operators / lgb_plan_propagate is
+ *    a DEVICE pointer owned by the caller.  The plan owns its workspace.
+ *  - Every call returns an lgb status code; nothing throws across the ABI and
+ *    no device code traps.  Per-instance failures (a non-finite state) are
+ *    reported through lgb_plan_errors.
+ *  - One plan per stream at a time; distinct plans are independent.
+ */
+#ifndef LINDBLAD_GB300_H
+#define LINDBLAD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  LGB_OK = 0,
+  LGB_ERR_INVALID_ARG = 1,  /* bad size, null pointer, unsupported combination */
+  LGB_ERR_UNSUPPORTED = 2,  /* valid request this build cannot serve            */
+  LGB_ERR_CUDA = 3,         /* a CUDA runtime call failed                        */
+  LGB_ERR_NONFINITE = 4,    /* some instance's state became NaN/Inf              */
+  LGB_ERR_TIMEOUT = 5,      /* a bounded device wait gave up                     */
+  LGB_ERR_NO_DEVICE = 6,    /* no CUDA device visible                            */
+  LGB_ERR_STATE = 7         /* call order violated (e.g. propagate before set)   */
+};
+
+/* ---- precisions ------------------------------------------------------------ */
+enum {
+  LGB_PREC_FP64 = 0,    /* complex128 arithmetic: the check path               */
+  LGB_PREC_FP32 = 1,    /* complex64 arithmetic on the FP32 pipes ("plain")    */
+  LGB_PREC_TF32X3 = 2,  /* split 3xTF32 tensor-core products, FP32 accumulate  */
+  LGB_PREC_BF16X3 = 3   /* split 3xBF16 tensor-core products, FP32 accumulate  */
+};
+
+/* ---- collapse-operator storage -------------------------------------------- */
+enum {
+  LGB_COPS_NONE = 0,
+  LGB_COPS_DENSE = 1,  /* n_cops dense N x N operators per instance            */
+  LGB_COPS_DIAG = 2    /* n_cops diagonals (length N) per instance             */
+};
+
+/* ---- schedules ----------------------------------------------------------------- */
+enum {
+  LGB_SCHED_AUTO = 0,
+  LGB_SCHED_CTA = 1,   /* one CTA holds an instance in shared memory for all steps */
+  LGB_SCHED_GEMM = 2   /* grid-wide tiled complex GEMMs per RK4 stage               */
+};
+
+typedef struct lgb_plan* lgb_plan_t;
+
+/* Problem description, copied by lgb_plan_create. */
+typedef struct {
+  int32_t n_inst;       /* number of independent instances (>= 1)                */
+  int32_t n_cops;       /* collapse operators per instance                        */
+  int32_t cops_kind;    /* LGB_COPS_*                                              */
+  int32_t n_eops;       /* observables per instance (<= 16)                        */
+  int32_t n_drive;      /* drive terms: H(t) = H0 - sum_i f_i(t) H_i (<= 4)        */
+  int32_t nt;           /* RK4 steps (>= 0)                                        */
+  int32_t obs_t0;       /* 1: observable row 0 holds Tr[O rho0] (Nt+1 rows)        */
+  int32_t store_every;  /* store the state every s steps into states_out (0: no)  */
+  int32_t precision;    /* LGB_PREC_*                                              */
+  int32_t schedule;     /* LGB_SCHED_*                                             */
+  int32_t drive_shared; /* 1: one sample set f_i(t_k) for all instances           */
+  int32_t flags;        /* reserved, must be 0                                     */
+  double dt;            /* time step                                               */
+} lgb_problem_t;
+
+/* Library version: major*10000 + minor*100 + patch. */
+int lgb_get_version(void);
+
+/* Static, human-readable text for a status code. */
+const char* lgb_status_string(int status);
+
+/* Create a plan for a batch.  dims_host[n_inst] are the instance dimensions
+ * (host memory).  Chooses the schedule, sorts the instances by cost and
+ * allocates the device workspace on the current device.
+ * Replaces the set-up half of LindbladSolver.__init__/run
+ * (pyqed/oqs.py:1115-1147, 1149-1187). */
+int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_t* dims_host);
+
+/* Release the plan and its workspace. */
+int lgb_plan_destroy(lgb_plan_t plan);
+
+/* Upload the operators (device pointers, packed layout, complex128):
+ *   H         Hamiltonian (static part H0 when n_drive > 0)       required
+ *   cops      collapse operators (dense or diagonals)              if n_cops > 0
+ *   eops      observables                                          if n_eops > 0
+ *   drive_ops H_1..H_n_drive of H(t) = H0 - sum_i f_i(t) H_i       if n_drive > 0
+ * Forms H_eff = H - (i/2) sum_k L_k^dag L_k once, in the plan's precision.
+ * Replaces the operator set-up of liouvillian/lindbladian
+ * (pyqed/oqs.py:697-715) that the reference repeats at every RHS call. */
+int lgb_plan_set_operators(lgb_plan_t plan, const double* H, const double* cops,
+                           const double* eops, const double* drive_ops, void* stream);
+
+/* Propagate nt RK4 steps from rho0 (device, packed complex128).
+ *   drive_samples  f_i(t0 + (k+1) dt), k = 0..nt-1: [n_drive][nt] when
+ *                  drive_shared, else [n_inst][n_drive][nt] (doubles)
+ *   obs_out        [n_inst][nt + obs_t0][n_eops] complex128, or NULL
+ *   rho_out        final states, packed complex128, or NULL
+ *   states_out     [per instance: nt/store_every states of N x N], or NULL
+ * Replaces the time loops of _lindblad (pyqed/oqs.py:1596-1696),
+ * _lindblad_driven (pyqed/oqs.py:1699-1806), _fast_lindblad
+ * (pyqed/oqs.py:1492-1594) and _correlation_2p_1t (pyqed/oqs.py:717-791),
+ * with rk4 (pyqed/phys.py:1051-1064) and obs_dm (pyqed/phys.py:1257-1264)
+ * fused into the kernels.  Asynchronous on `stream`. */
+int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_samples,
+                       double* obs_out, double* rho_out, double* states_out, void* stream);
+
+/* Copy the per-instance status flags (LGB_OK or LGB_ERR_NONFINITE /
+ * LGB_ERR_TIMEOUT) of the last propagate into flags_host[n_inst];
+ * synchronises the plan's last stream.  Returns the first non-OK flag. */
+int lgb_plan_errors(lgb_plan_t plan, int32_t* flags_host);
+
+/* Plan introspection: the schedule and precision in use, the bytes of
+ * device workspace, the dynamic shared memory per CTA and the number of
+ * kernel launches one propagate issues. */
+typedef struct {
+  int32_t schedule;
+  int32_t precision;
+  int32_t smem_bytes;
+  int32_t launches_per_propagate;
+  int64_t workspace_bytes;
+  int64_t flops_per_step;   /* algorithmic real flops of one RK4 step, whole batch */
+} lgb_plan_info_t;
+
+int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LINDBLAD_GB300_H */

@@ -1,0 +1,113 @@
+"""ctypes binding of the C ABI declared in ``include/lindblad_gb300.h``.
+
+This is the binding a maintainer of the reference would add beside
+``pyqed/oqs.py``: plain pointers and sizes, device memory held by torch
+tensors, status codes turned into ``LindbladError``.  The library is loaded
+from the package tree (``pyqed_gb300/_lib``); if it is missing the product
+path raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "_lib", "liblindblad_gb300.so")
+
+# status codes
+LGB_OK = 0
+LGB_ERR_INVALID_ARG = 1
+LGB_ERR_UNSUPPORTED = 2
+LGB_ERR_CUDA = 3
+LGB_ERR_NONFINITE = 4
+LGB_ERR_TIMEOUT = 5
+LGB_ERR_NO_DEVICE = 6
+LGB_ERR_STATE = 7
+
+# precisions
+PREC = {"fp64": 0, "fp32": 1, "3xtf32": 2, "3xbf16": 3}
+PREC_NAME = {v: k for k, v in PREC.items()}
+# collapse-operator storage
+COPS_NONE, COPS_DENSE, COPS_DIAG = 0, 1, 2
+# schedules
+SCHED = {"auto": 0, "cta": 1, "gemm": 2}
+SCHED_NAME = {v: k for k, v in SCHED.items()}
+
+# Every symbol include/lindblad_gb300.h declares.
+EXPORTS = [
+    "lgb_get_version", "lgb_status_string", "lgb_plan_create", "lgb_plan_destroy",
+    "lgb_plan_set_operators", "lgb_plan_propagate", "lgb_plan_errors", "lgb_plan_get_info",
+]
+
+
+class LindbladError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = _status_text(status)
+        super().__init__("%s: %s (status %d)" % (what, msg, status) if what else msg)
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [
+        ("n_inst", ctypes.c_int32), ("n_cops", ctypes.c_int32), ("cops_kind", ctypes.c_int32),
+        ("n_eops", ctypes.c_int32), ("n_drive", ctypes.c_int32), ("nt", ctypes.c_int32),
+        ("obs_t0", ctypes.c_int32), ("store_every", ctypes.c_int32),
+        ("precision", ctypes.c_int32), ("schedule", ctypes.c_int32),
+        ("drive_shared", ctypes.c_int32), ("flags", ctypes.c_int32), ("dt", ctypes.c_double),
+    ]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [
+        ("schedule", ctypes.c_int32), ("precision", ctypes.c_int32),
+        ("smem_bytes", ctypes.c_int32), ("launches_per_propagate", ctypes.c_int32),
+        ("workspace_bytes", ctypes.c_int64), ("flops_per_step", ctypes.c_int64),
+    ]
+
+
+_lib = None
+
+
+def _status_text(status):
+    try:
+        return lib().lgb_status_string(status).decode()
+    except Exception:  # library not loadable: still produce a message
+        return "status %d" % status
+
+
+def lib():
+    """Load (once) and return the CUDA library; raise if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBPATH):
+        raise RuntimeError(
+            "pyqed_gb300 CUDA library not found at %s; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` or "
+            "`python -m pyqed_gb300.build`" % LIBPATH)
+    L = ctypes.CDLL(LIBPATH)
+    vp, i32, dp = ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p
+    L.lgb_get_version.restype = ctypes.c_int
+    L.lgb_get_version.argtypes = []
+    L.lgb_status_string.restype = ctypes.c_char_p
+    L.lgb_status_string.argtypes = [ctypes.c_int]
+    L.lgb_plan_create.restype = ctypes.c_int
+    L.lgb_plan_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(Problem),
+                                  ctypes.POINTER(i32)]
+    L.lgb_plan_destroy.restype = ctypes.c_int
+    L.lgb_plan_destroy.argtypes = [vp]
+    L.lgb_plan_set_operators.restype = ctypes.c_int
+    L.lgb_plan_set_operators.argtypes = [vp, dp, dp, dp, dp, vp]
+    L.lgb_plan_propagate.restype = ctypes.c_int
+    L.lgb_plan_propagate.argtypes = [vp, dp, dp, dp, dp, dp, vp]
+    L.lgb_plan_errors.restype = ctypes.c_int
+    L.lgb_plan_errors.argtypes = [vp, ctypes.POINTER(i32)]
+    L.lgb_plan_get_info.restype = ctypes.c_int
+    L.lgb_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+    _lib = L
+    return L
+
+
+def check(status, what=""):
+    if status != LGB_OK:
+        raise LindbladError(status, what)

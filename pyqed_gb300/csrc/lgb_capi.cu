@@ -1,0 +1,312 @@
+// C-ABI entry points (include/lindblad_gb300.h): plan set-up, operator
+// upload, propagation and error reporting.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+
+#include "lgb_internal.h"
+
+using lgb::CtaParams;
+
+namespace {
+
+constexpr int kVersion = 1 * 10000 + 0 * 100 + 0;
+constexpr int kSmemBudget = 224 * 1024;  // dynamic shared memory per CTA we plan with
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? LGB_OK : LGB_ERR_CUDA; }
+
+template <typename P>
+int dalloc(lgb_plan* pl, P** ptr, size_t bytes) {
+  *ptr = nullptr;
+  if (bytes == 0) return LGB_OK;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) return LGB_ERR_CUDA;
+  pl->allocations.push_back(p);
+  pl->ws_bytes += bytes;
+  *ptr = reinterpret_cast<P*>(p);
+  return LGB_OK;
+}
+
+template <typename T>
+int upload(lgb_plan* pl, T** dptr, const std::vector<T>& v) {
+  int s = dalloc(pl, dptr, v.size() * sizeof(T));
+  if (s != LGB_OK || v.empty()) return s;
+  return cuda_status(cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+void free_plan(lgb_plan* pl) {
+  for (void* p : pl->allocations) cudaFree(p);
+  pl->allocations.clear();
+}
+
+int validate(const lgb_problem_t* pr, const int32_t* dims) {
+  if (pr == nullptr || dims == nullptr) return LGB_ERR_INVALID_ARG;
+  if (pr->n_inst < 1 || pr->n_cops < 0 || pr->n_eops < 0 || pr->n_eops > 16 || pr->n_drive < 0 ||
+      pr->n_drive > 4 || pr->nt < 0 || pr->store_every < 0 || pr->flags != 0)
+    return LGB_ERR_INVALID_ARG;
+  if (pr->cops_kind < LGB_COPS_NONE || pr->cops_kind > LGB_COPS_DIAG) return LGB_ERR_INVALID_ARG;
+  if (pr->cops_kind == LGB_COPS_NONE && pr->n_cops != 0) return LGB_ERR_INVALID_ARG;
+  if (pr->cops_kind != LGB_COPS_NONE && pr->n_cops == 0) return LGB_ERR_INVALID_ARG;
+  if (pr->precision < LGB_PREC_FP64 || pr->precision > LGB_PREC_BF16X3) return LGB_ERR_INVALID_ARG;
+  if (pr->schedule < LGB_SCHED_AUTO || pr->schedule > LGB_SCHED_GEMM) return LGB_ERR_INVALID_ARG;
+  if (!(pr->dt == pr->dt)) return LGB_ERR_INVALID_ARG;
+  for (int b = 0; b < pr->n_inst; ++b)
+    if (dims[b] < 1 || dims[b] > 65536) return LGB_ERR_INVALID_ARG;
+  return LGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgb_get_version(void) { return kVersion; }
+
+const char* lgb_status_string(int status) {
+  switch (status) {
+    case LGB_OK: return "ok";
+    case LGB_ERR_INVALID_ARG: return "invalid argument";
+    case LGB_ERR_UNSUPPORTED: return "unsupported by this build";
+    case LGB_ERR_CUDA: return "CUDA runtime error";
+    case LGB_ERR_NONFINITE: return "state became non-finite";
+    case LGB_ERR_TIMEOUT: return "bounded device wait timed out";
+    case LGB_ERR_NO_DEVICE: return "no CUDA device";
+    case LGB_ERR_STATE: return "call order violated";
+    default: return "unknown status";
+  }
+}
+
+int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_t* dims_host) {
+  if (plan == nullptr) return LGB_ERR_INVALID_ARG;
+  *plan = nullptr;
+  int s = validate(problem, dims_host);
+  if (s != LGB_OK) return s;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return LGB_ERR_NO_DEVICE;
+  }
+  lgb_plan* pl = new (std::nothrow) lgb_plan();
+  if (pl == nullptr) return LGB_ERR_INVALID_ARG;
+  pl->prob = *problem;
+  cudaGetDevice(&pl->device);
+  const lgb_problem_t& pr = pl->prob;
+  const int n = pr.n_inst;
+  const int prec = pr.precision;
+  const size_t esz = lgb::cta_elem_bytes(prec == LGB_PREC_FP64 ? 0 : 1);
+  pl->padc = (int)(16 / esz);
+
+  pl->dims.assign(dims_host, dims_host + n);
+  pl->npad.resize(n);
+  pl->off.resize(n);
+  pl->doff.resize(n);
+  pl->woff.resize(n);
+  pl->soff.resize(n);
+  pl->place.assign(n, 0);
+  pl->n_store = pr.store_every > 0 ? pr.nt / pr.store_every : 0;
+  const int K = pr.n_cops;
+  const bool dense = pr.cops_kind == LGB_COPS_DENSE;
+  int maxnp = 0;
+  for (int b = 0; b < n; ++b) {
+    const long long N = pl->dims[b];
+    const int NP = (int)((N + 3) / 4 * 4);
+    pl->npad[b] = NP;
+    maxnp = std::max(maxnp, NP);
+    pl->off[b] = pl->tot_off;
+    pl->doff[b] = pl->tot_doff;
+    pl->woff[b] = pl->tot_woff;
+    pl->soff[b] = pl->n_store * pl->tot_off;
+    pl->tot_off += N * N;
+    pl->tot_doff += N;
+    pl->tot_woff += (long long)NP * (NP + pl->padc);
+    pl->flops_per_step += 64LL * (1 + (dense ? K : 0)) * N * N * N;
+  }
+
+  // ---- schedule ---------------------------------------------------------------
+  // The CTA-resident kernel needs A^T, X, X^T (+ dense-collapse scratch) in
+  // shared memory; anything larger goes to the grid-wide GEMM schedule.
+  int sched = pr.schedule;
+  bool cta_ok = maxnp <= lgb::cta_max_npad();
+  int smem = 0;
+  if (cta_ok) {
+    for (int b = 0; b < n; ++b) {
+      const long long ms = (long long)pl->npad[b] * (pl->npad[b] + pl->padc) * esz;
+      long long used = 3 * ms;
+      unsigned char pf = 0;
+      if (used > kSmemBudget) {
+        cta_ok = false;
+        break;
+      }
+      if (dense) {
+        if (used + K * ms <= kSmemBudget) {
+          used += K * ms;
+          pf |= 2;
+        }
+        if (used + K * ms <= kSmemBudget) {
+          used += K * ms;
+          pf |= 1;
+        }
+      }
+      pl->place[b] = pf;
+      smem = std::max<long long>(smem, used);
+    }
+  }
+  if (sched == LGB_SCHED_AUTO) sched = cta_ok ? LGB_SCHED_CTA : LGB_SCHED_GEMM;
+  if (sched == LGB_SCHED_CTA && !cta_ok) {
+    delete pl;
+    return LGB_ERR_UNSUPPORTED;
+  }
+  if (sched == LGB_SCHED_GEMM || prec == LGB_PREC_TF32X3 || prec == LGB_PREC_BF16X3) {
+    delete pl;
+    return LGB_ERR_UNSUPPORTED;
+  }
+  pl->schedule = sched;
+  pl->smem_bytes = smem;
+
+  // Largest instances first: with one CTA per instance the hardware block
+  // scheduler then performs longest-processing-time-first list scheduling.
+  pl->order.resize(n);
+  std::iota(pl->order.begin(), pl->order.end(), 0);
+  std::stable_sort(pl->order.begin(), pl->order.end(),
+                   [&](int a, int c) { return pl->npad[a] > pl->npad[c]; });
+
+  // ---- device buffers ---------------------------------------------------------
+  s = LGB_OK;
+  const long long W = pl->tot_woff;
+  s = s ? s : upload(pl, &pl->d_dims, pl->dims);
+  s = s ? s : upload(pl, &pl->d_npad, pl->npad);
+  s = s ? s : upload(pl, &pl->d_order, pl->order);
+  s = s ? s : upload(pl, &pl->d_off, pl->off);
+  s = s ? s : upload(pl, &pl->d_doff, pl->doff);
+  s = s ? s : upload(pl, &pl->d_woff, pl->woff);
+  s = s ? s : upload(pl, &pl->d_soff, pl->soff);
+  s = s ? s : upload(pl, &pl->d_place, pl->place);
+  s = s ? s : dalloc(pl, &pl->d_shift, n * sizeof(double));
+  s = s ? s : dalloc(pl, &pl->d_At, W * esz);
+  s = s ? s : dalloc(pl, &pl->d_Lt, dense ? (size_t)K * W * esz : 0);
+  s = s ? s : dalloc(pl, &pl->d_Dm, pr.cops_kind == LGB_COPS_DIAG ? W * esz : 0);
+  s = s ? s : dalloc(pl, &pl->d_Gt, (size_t)pr.n_drive * W * esz);
+  s = s ? s : dalloc(pl, &pl->d_Ot, (size_t)pr.n_eops * W * sizeof(double2));
+  s = s ? s : dalloc(pl, &pl->d_state, 2 * W * esz);
+  s = s ? s : dalloc(pl, &pl->d_y, dense ? (size_t)K * W * esz : 0);
+  s = s ? s : dalloc(pl, &pl->d_err, n * sizeof(int));
+  if (s == LGB_OK && pl->d_err) s = cuda_status(cudaMemset(pl->d_err, 0, n * sizeof(int)));
+  if (s != LGB_OK) {
+    free_plan(pl);
+    delete pl;
+    return s;
+  }
+  *plan = pl;
+  return LGB_OK;
+}
+
+int lgb_plan_destroy(lgb_plan_t plan) {
+  if (plan == nullptr) return LGB_ERR_INVALID_ARG;
+  free_plan(plan);
+  delete plan;
+  return LGB_OK;
+}
+
+int lgb_plan_set_operators(lgb_plan_t plan, const double* H, const double* cops,
+                           const double* eops, const double* drive_ops, void* stream) {
+  if (plan == nullptr || H == nullptr) return LGB_ERR_INVALID_ARG;
+  const lgb_problem_t& pr = plan->prob;
+  if (pr.n_cops > 0 && cops == nullptr) return LGB_ERR_INVALID_ARG;
+  if (pr.n_eops > 0 && eops == nullptr) return LGB_ERR_INVALID_ARG;
+  if (pr.n_drive > 0 && drive_ops == nullptr) return LGB_ERR_INVALID_ARG;
+  lgb::SetupParams sp{};
+  sp.n_inst = pr.n_inst;
+  sp.n_cops = pr.n_cops;
+  sp.cops_kind = pr.cops_kind;
+  sp.n_eops = pr.n_eops;
+  sp.n_drive = pr.n_drive;
+  sp.padc = plan->padc;
+  sp.dims = plan->d_dims;
+  sp.npad = plan->d_npad;
+  sp.off = plan->d_off;
+  sp.doff = plan->d_doff;
+  sp.woff = plan->d_woff;
+  sp.H = reinterpret_cast<const double2*>(H);
+  sp.cops = reinterpret_cast<const double2*>(cops);
+  sp.eops = reinterpret_cast<const double2*>(eops);
+  sp.dops = reinterpret_cast<const double2*>(drive_ops);
+  sp.shift = plan->d_shift;
+  sp.At = plan->d_At;
+  sp.Lt = plan->d_Lt;
+  sp.Dm = plan->d_Dm;
+  sp.Gt = plan->d_Gt;
+  sp.Ot = plan->d_Ot;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int s = cuda_status(lgb::launch_setup(sp, pr.precision == LGB_PREC_FP64 ? 0 : 1, st));
+  if (s == LGB_OK) plan->ops_set = true;
+  plan->last_stream = st;
+  return s;
+}
+
+int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_samples,
+                       double* obs_out, double* rho_out, double* states_out, void* stream) {
+  if (plan == nullptr || rho0 == nullptr) return LGB_ERR_INVALID_ARG;
+  if (!plan->ops_set) return LGB_ERR_STATE;
+  const lgb_problem_t& pr = plan->prob;
+  if (pr.n_drive > 0 && pr.nt > 0 && drive_samples == nullptr) return LGB_ERR_INVALID_ARG;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  plan->last_stream = st;
+  CtaParams p{};
+  p.n_inst = pr.n_inst;
+  p.n_cops = pr.n_cops;
+  p.cops_kind = pr.cops_kind;
+  p.n_eops = pr.n_eops;
+  p.n_drive = pr.n_drive;
+  p.nt = pr.nt;
+  p.obs_t0 = pr.obs_t0;
+  p.store_every = pr.store_every;
+  p.drive_shared = pr.drive_shared;
+  p.dt = pr.dt;
+  p.order = plan->d_order;
+  p.dims = plan->d_dims;
+  p.npad = plan->d_npad;
+  p.off = plan->d_off;
+  p.woff = plan->d_woff;
+  p.soff = plan->d_soff;
+  p.place = plan->d_place;
+  p.At = plan->d_At;
+  p.Lt = plan->d_Lt;
+  p.Dm = plan->d_Dm;
+  p.Gt = plan->d_Gt;
+  p.Ot = plan->d_Ot;
+  p.drive = drive_samples;
+  p.rho0 = reinterpret_cast<const double2*>(rho0);
+  p.obs_out = reinterpret_cast<double2*>(obs_out);
+  p.rho_out = reinterpret_cast<double2*>(rho_out);
+  p.states_out = reinterpret_cast<double2*>(states_out);
+  p.state_ws = plan->d_state;
+  p.y_ws = plan->d_y;
+  p.err = plan->d_err;
+  p.smem_bytes = plan->smem_bytes;
+  return cuda_status(lgb::launch_cta_rk4(p, pr.precision == LGB_PREC_FP64 ? 0 : 1, pr.n_inst, st));
+}
+
+int lgb_plan_errors(lgb_plan_t plan, int32_t* flags_host) {
+  if (plan == nullptr || flags_host == nullptr) return LGB_ERR_INVALID_ARG;
+  cudaError_t e = cudaStreamSynchronize(plan->last_stream);
+  if (e != cudaSuccess) return LGB_ERR_CUDA;
+  e = cudaMemcpy(flags_host, plan->d_err, plan->prob.n_inst * sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return LGB_ERR_CUDA;
+  for (int b = 0; b < plan->prob.n_inst; ++b)
+    if (flags_host[b] != LGB_OK) return flags_host[b];
+  return LGB_OK;
+}
+
+int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
+  if (plan == nullptr || info == nullptr) return LGB_ERR_INVALID_ARG;
+  info->schedule = plan->schedule;
+  info->precision = plan->prob.precision;
+  info->smem_bytes = plan->smem_bytes;
+  info->launches_per_propagate = 1;
+  info->workspace_bytes = (int64_t)plan->ws_bytes;
+  info->flops_per_step = plan->flops_per_step;
+  return LGB_OK;
+}
+
+}  // extern "C"

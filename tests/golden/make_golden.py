@@ -1,0 +1,151 @@
+"""Generate the golden fixtures from the reference implementation itself.
+
+Run in a container where the reference (binggu56/pyqed 0.1.3) is mounted at
+``/root/reference``:
+
+    python tests/golden/make_golden.py
+
+Every fixture holds the inputs (or, for N >= 256, a checksum of the seeded
+inputs) and the outputs of the reference's own entry points:
+
+* ``jc16.npz``       ``LindbladSolver.run`` (CSR path, ``pyqed/oqs.py:1149-1187``
+                     -> ``_lindblad`` ``pyqed/oqs.py:1596-1696``), full 2000 steps.
+* ``gue64.npz``      ``_fast_lindblad`` (``pyqed/oqs.py:1492-1594``), N=64, K=4.
+* ``gue256.npz``     ``_fast_lindblad``, the N=256, K=4 workload, 4 steps.
+* ``gue1024.npz``    ``_fast_lindblad``, the N=1024, K=8 workload, 2 steps
+                     (rows 0..7, the diagonal and the trace of the final state).
+* ``exciton.npz``    ``_correlation_2p_1t`` (``pyqed/oqs.py:717-791``) on 8
+                     instances of the exciton batch, 40 steps.
+* ``driven64.npz``   ``LindbladSolver.run`` with ``H = [H0, [mu, f]]``
+                     (``_lindblad_driven``, ``pyqed/oqs.py:1699-1806``), 2
+                     instances of the driven batch, 30 steps.
+* ``corr_jc.npz``    ``correlation_2op_1t``, ``correlation_3op_1t`` and
+                     ``correlation_4op_1t`` (``pyqed/oqs.py:1193-1312``) on the
+                     Jaynes-Cummings system, 50 steps.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+import tempfile
+
+import numpy as np
+from scipy.sparse import csr_matrix
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+from pyqed_gb300 import workloads as W  # noqa: E402
+from ref_loader import load  # noqa: E402
+
+
+def digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype=np.complex128).tobytes())
+    return h.hexdigest()
+
+
+def main():
+    oqs = load()
+    out = {}
+
+    # 1. Jaynes-Cummings via the public run() (CSR operators, as it requires)
+    jc = W.jaynes_cummings()
+    sol = oqs.LindbladSolver(csr_matrix(jc["H"]), [csr_matrix(c) for c in jc["c_ops"]])
+    r = sol.run(jc["rho0"], dt=jc["dt"], Nt=jc["nt"], e_ops=[csr_matrix(e) for e in jc["e_ops"]])
+    keep = [0, 499, 1999]
+    out["jc16"] = dict(
+        H=jc["H"], c_ops=np.stack(jc["c_ops"]), rho0=jc["rho0"], e_ops=np.stack(jc["e_ops"]),
+        dt=jc["dt"], nt=jc["nt"], observables=r.observables, times=r.times,
+        state_index=np.array(keep), states=np.stack([r.rholist[k].toarray() for k in keep]))
+
+    # 2. GUE N=64, K=4, dense path
+    g = W.gue_instance(N=64, K=4, seed=12, nt=50)
+    rho = oqs._fast_lindblad(g["H"], g["rho0"].copy(), g["c_ops"], e_ops=[], Nt=g["nt"], dt=g["dt"])
+    out["gue64"] = dict(H=g["H"], c_ops=np.stack(g["c_ops"]), rho0=g["rho0"], dt=g["dt"],
+                        nt=g["nt"], rho=rho)
+
+    # 3. GUE N=256, K=4 (the workload's own seed), 4 steps
+    g = W.gue_instance(N=256, K=4, seed=2)
+    nt = 4
+    rho = oqs._fast_lindblad(g["H"], g["rho0"].copy(), g["c_ops"], e_ops=[], Nt=nt, dt=g["dt"])
+    out["gue256"] = dict(digest=digest(g["H"], *g["c_ops"], g["rho0"]), dt=g["dt"], nt=nt, rho=rho)
+
+    # 4. GUE N=1024, K=8, rank-4 rho0, 2 steps (slices only)
+    g = W.gue_instance(N=1024, K=8, scale=0.02, rank=4, seed=4, dt=0.005, nt=1000)
+    nt = 2
+    rho = oqs._fast_lindblad(g["H"], g["rho0"].copy(), g["c_ops"], e_ops=[], Nt=nt, dt=g["dt"])
+    out["gue1024"] = dict(digest=digest(g["H"], *g["c_ops"], g["rho0"]), dt=g["dt"], nt=nt,
+                          rows=rho[:8, :], diag=np.diag(rho).copy(), trace=np.trace(rho),
+                          fro=np.linalg.norm(rho))
+
+    # 5. exciton correlation functions, 8 instances spanning n = 8..64
+    dims = W.exciton_dims()
+    want = [9, 17, 24, 33, 40, 49, 57, 65]
+    idx = [int(np.nonzero(dims == n)[0][0]) for n in want]
+    ex = W.exciton_batch(indices=idx, nt=40)
+    cors = []
+    with tempfile.TemporaryDirectory() as td:
+        for i in range(len(idx)):
+            cops = [np.diag(c) for c in ex["c_diag"][i]]
+            cors.append(oqs._correlation_2p_1t(ex["H"][i], ex["rho_g"][i], [ex["mu"][i], ex["mu"][i]],
+                                               cops, ex["dt"], ex["nt"],
+                                               output=os.path.join(td, "cor.dat")))
+    Nmax = max(want)
+    Hp = np.zeros((len(idx), Nmax, Nmax), complex)
+    Mp = np.zeros_like(Hp)
+    for i, n in enumerate(want):
+        Hp[i, :n, :n] = ex["H"][i]
+        Mp[i, :n, :n] = ex["mu"][i]
+    out["exciton"] = dict(indices=np.array(idx), dims=np.array(want), H=Hp, mu=Mp,
+                          dt=ex["dt"], nt=ex["nt"], cor=np.stack(cors))
+
+    # 6. driven instances through run() with a list Hamiltonian
+    d = W.driven_batch(n_inst=2, nt=30)
+    obs_all, rho_all = [], []
+    for b in range(2):
+        E = d["E"]
+
+        def f(t, E=E, dt=d["dt"]):
+            return E[int(round(t / dt)) - 1]
+        Lk = [np.sqrt(d["gamma"][b][k]) * d["L"][b][k] for k in range(2)]
+        sol = oqs.LindbladSolver([csr_matrix(d["H0"][b]), [csr_matrix(d["mu"][b]), f]],
+                                 [csr_matrix(L) for L in Lk])
+        r = sol.run(d["rho0"][b], dt=d["dt"], Nt=d["nt"], e_ops=[csr_matrix(d["O"][b])])
+        obs_all.append(r.observables[:, 0])
+        rho_all.append(r.rholist[-1].toarray())
+    out["driven64"] = dict(
+        H0=np.stack(d["H0"][:2]), mu=np.stack(d["mu"][:2]),
+        L=np.stack([np.stack([np.sqrt(d["gamma"][b][k]) * d["L"][b][k] for k in range(2)])
+                    for b in range(2)]),
+        rho0=np.stack(d["rho0"][:2]), O=np.stack(d["O"][:2]), E=d["E"], dt=d["dt"], nt=d["nt"],
+        observables=np.stack(obs_all), rho=np.stack(rho_all))
+
+    # 7. correlation entry points on the JC system
+    jc = W.jaynes_cummings()
+    Hs, cs = csr_matrix(jc["H"]), [csr_matrix(c) for c in jc["c_ops"]]
+    a = np.kron(np.diag(np.sqrt(np.arange(1, 8)), 1), np.eye(2)).astype(complex)
+    sm = np.kron(np.eye(8), np.array([[0, 1], [0, 0]], complex))
+    ad, sp = a.conj().T, sm.conj().T
+    sol = oqs.LindbladSolver(Hs, cs)
+    with tempfile.TemporaryDirectory() as td:
+        fn = os.path.join(td, "cor.dat")
+        c2 = sol.correlation_2op_1t(jc["rho0"], ad, a, dt=0.02, Nt=50, output=fn)
+        cor_dat = open(fn).read()
+    c3 = sol.correlation_3op_1t(jc["rho0"], [csr_matrix(ad), csr_matrix(a @ ad), csr_matrix(a)],
+                                dt=0.02, Nt=50)
+    c4 = sol.correlation_4op_1t(jc["rho0"], [csr_matrix(ad), csr_matrix(sp), csr_matrix(sm),
+                                             csr_matrix(a)], dt=0.02, nt=50)
+    out["corr_jc"] = dict(a=a, sm=sm, c2=c2, c3=c3, c4=c4, cor_dat=np.array(cor_dat))
+
+    for name, arrs in out.items():
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **arrs)
+        print(name, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

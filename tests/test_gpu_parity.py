@@ -1,0 +1,176 @@
+"""GPU parity: the CUDA propagator against the reference's own outputs
+(tests/golden, produced by running binggu56/pyqed) and against the oracle on
+seeded inputs.
+
+Tolerances: 1e-12 max-abs for the FP64 path; 1e-5 max-abs on rho(t) (and on
+C(t) relative to max|C|) for the FP32 and split-precision paths.
+"""
+import os
+
+import numpy as np
+import pytest
+from scipy.sparse import csr_matrix
+
+from oracle import lindblad_oracle as O
+from pyqed_gb300 import LindbladSolver, correlation_batch, propagate_batch
+from pyqed_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pyqed_gb300.build import build
+    build()
+
+
+# ---- golden fixtures (reference outputs) ----------------------------------------
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_jc16_run_golden(golden, prec, tol):
+    g = golden("jc16")
+    sol = LindbladSolver(csr_matrix(g["H"]), [csr_matrix(c) for c in g["c_ops"]])
+    r = sol.run(g["rho0"], dt=float(g["dt"]), Nt=int(g["nt"]),
+                e_ops=[csr_matrix(e) for e in g["e_ops"]], precision=prec)
+    assert r.observables.shape == (2001, 2)
+    assert len(r.rholist) == 2000 and r.times.shape == (2001,)
+    assert np.abs(r.observables - g["observables"]).max() < tol
+    for k, s in zip(g["state_index"], g["states"]):
+        assert np.abs(r.rholist[k].toarray() - s).max() < tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_gue64_evolve_fast_golden(golden, prec, tol):
+    g = golden("gue64")
+    sol = LindbladSolver(g["H"], list(g["c_ops"]))
+    rho0 = g["rho0"].copy()
+    rho = sol.evolve_fast(rho0, dt=float(g["dt"]), Nt=int(g["nt"]), e_ops=[], precision=prec)
+    assert np.abs(rho - g["rho"]).max() < tol
+    assert np.abs(rho0 - g["rho"]).max() < tol  # the reference overwrites rho0 too
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_exciton_correlation_golden(golden, prec, tol):
+    g = golden("exciton")
+    ex = W.exciton_batch(indices=[int(i) for i in g["indices"]], nt=int(g["nt"]))
+    cops = [[np.diag(c) for c in cd] for cd in ex["c_diag"]]
+    C = correlation_batch(ex["H"], cops, ex["rho_g"], ex["mu"], ex["mu"], ex["dt"], ex["nt"],
+                          precision=prec)
+    ref = g["cor"]
+    err = np.abs(C - ref).max() / np.abs(ref).max()
+    assert err < tol, err
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_driven_run_golden(golden, prec, tol):
+    g = golden("driven64")
+    dt, nt = float(g["dt"]), int(g["nt"])
+    for b in range(2):
+        E = g["E"]
+        sol = LindbladSolver([csr_matrix(g["H0"][b]), [csr_matrix(g["mu"][b]),
+                              lambda t, E=E: E[int(round(t / dt)) - 1]]],
+                             [csr_matrix(L) for L in g["L"][b]])
+        r = sol.run(g["rho0"][b], dt=dt, Nt=nt, e_ops=[csr_matrix(g["O"][b])], precision=prec)
+        assert r.observables.shape == (nt, 1)
+        assert np.abs(r.observables[:, 0] - g["observables"][b]).max() < tol
+        assert np.abs(r.rholist[-1].toarray() - g["rho"][b]).max() < tol
+
+
+def test_correlation_entry_points_golden(golden, tmp_path):
+    g = golden("corr_jc")
+    jc = W.jaynes_cummings()
+    a, sm = g["a"], g["sm"]
+    ad, sp = a.conj().T, sm.conj().T
+    sol = LindbladSolver(jc["H"], jc["c_ops"])
+    fn = str(tmp_path / "cor.dat")
+    c2 = sol.correlation_2op_1t(jc["rho0"], ad, a, dt=0.02, Nt=50, output=fn)
+    assert np.abs(c2 - g["c2"]).max() < TOL64
+    # same file layout as the reference: "t C(t) " per line
+    ours = [l.split() for l in open(fn).read().splitlines()]
+    theirs = [l.split() for l in str(g["cor_dat"]).splitlines()]
+    assert len(ours) == len(theirs) == 50
+    assert all(o[0] == t[0] for o, t in zip(ours, theirs))
+    assert np.allclose([complex(o[1]) for o in ours], [complex(t[1]) for t in theirs],
+                       atol=1e-12, rtol=0)
+    c3 = sol.correlation_3op_1t(jc["rho0"], [ad, a @ ad, a], dt=0.02, Nt=50)
+    assert c3.shape == (51,) and np.abs(c3 - g["c3"]).max() < TOL64
+    c4 = sol.correlation_4op_1t(jc["rho0"], [ad, sp, sm, a], 0.02, 50)
+    assert np.abs(c4 - g["c4"]).max() < TOL64
+
+
+# ---- seeded cases against the oracle ----------------------------------------------
+
+def _random_instance(rng, N, K):
+    H = W.gue_matrix(rng, N)
+    cops = [(rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) * 0.05 / np.sqrt(N)
+            for _ in range(K)]
+    psi = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    psi /= np.linalg.norm(psi)
+    O_ = W.gue_matrix(rng, N)
+    return H, cops, np.outer(psi, psi.conj()), O_
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_uneven_batch_dense_cops_vs_oracle(prec, tol):
+    rng = np.random.default_rng(11)
+    dims = [1, 3, 5, 17, 33, 64, 65, 2] + ([88] if prec != "fp64" else [68])
+    insts = [_random_instance(rng, N, 2) for N in dims]
+    nt, dt = 12, 0.05
+    res = propagate_batch([i[0] for i in insts], [i[1] for i in insts], [i[2] for i in insts],
+                          dt, nt, e_ops=[[i[3]] for i in insts], obs_t0=True, precision=prec)
+    for b, (H, cops, rho0, O_) in enumerate(insts):
+        obs, states = O.lindblad(H, rho0, cops, [O_], Nt=nt, dt=dt)
+        assert np.abs(res["rho"][b] - states[-1]).max() < tol, (b, dims[b])
+        assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < tol * max(1, dims[b] ** 0.5)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_uneven_batch_diag_cops_nonhermitian_vs_oracle(prec, tol):
+    ex = W.exciton_batch(indices=list(range(24)), nt=30)
+    C = correlation_batch(ex["H"], [[np.diag(c) for c in cd] for cd in ex["c_diag"]],
+                          ex["rho_g"], ex["mu"], ex["mu"], ex["dt"], ex["nt"], precision=prec)
+    for i in range(24):
+        ref = O.propagate_diag_correlation(ex["H"][i], ex["mu"][i], ex["rho_g"][i],
+                                           ex["c_diag"][i], ex["dt"], ex["nt"])
+        assert np.abs(C[i] - ref).max() / np.abs(ref).max() < tol
+
+
+def test_no_cops_no_eops_and_zero_steps():
+    rng = np.random.default_rng(3)
+    H, _, rho0, _ = _random_instance(rng, 6, 0)
+    sol = LindbladSolver(H, None)
+    r = sol.run(rho0, dt=0.1, Nt=0, precision="fp64")
+    assert r.observables.shape == (1, 0) and r.rholist == []
+    r = sol.run(rho0, dt=0.1, Nt=5, precision="fp64", rholist_format="dense")
+    _, states = O.lindblad(H, rho0, [], [], Nt=5, dt=0.1)
+    assert np.abs(r.rholist[-1] - states[-1]).max() < TOL64
+
+
+def test_nonfinite_state_is_reported():
+    from pyqed_gb300._capi import LindbladError
+    rng = np.random.default_rng(4)
+    H, cops, rho0, _ = _random_instance(rng, 8, 1)
+    rho0 = rho0.copy()
+    rho0[2, 3] = np.nan
+    sol = LindbladSolver(H, cops)
+    with pytest.raises(LindbladError, match="non-finite"):
+        sol.run(rho0, dt=0.1, Nt=3, precision="fp32")
+
+
+def test_correlation_two_time_intended_semantics():
+    jc = W.jaynes_cummings()
+    a = np.kron(np.diag(np.sqrt(np.arange(1, 8)), 1), np.eye(2)).astype(complex)
+    ad = a.conj().T
+    sol = LindbladSolver(jc["H"], jc["c_ops"])
+    M = sol.correlation_3op_2t(jc["rho0"], [ad, a @ ad, a], 0.02, 4, 6)
+    assert M.shape == (4, 7)
+    _, states = O.lindblad(jc["H"], jc["rho0"], jc["c_ops"], [], Nt=4, dt=0.02)
+    for k in range(4):
+        ref = O.correlation_3op_1t(jc["H"], states[k], [ad, a @ ad, a], jc["c_ops"], 0.02, 6)
+        assert np.abs(M[k] - ref).max() < TOL64

@@ -1,0 +1,114 @@
+"""The oracle (numpy restatement) against the reference's own outputs.
+
+The fixtures under tests/golden were produced by running the reference
+(binggu56/pyqed) itself -- see tests/golden/make_golden.py.  CPU only.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from oracle import lindblad_oracle as O
+from pyqed_gb300 import workloads as W
+
+TOL = 1e-12
+
+
+def _digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype=np.complex128).tobytes())
+    return h.hexdigest()
+
+
+def test_jc16_run(golden):
+    g = golden("jc16")
+    obs, states = O.lindblad(g["H"], g["rho0"], list(g["c_ops"]), list(g["e_ops"]),
+                             Nt=int(g["nt"]), dt=float(g["dt"]))
+    assert obs.shape == g["observables"].shape == (2001, 2)
+    assert np.abs(obs - g["observables"]).max() < TOL
+    for k, s in zip(g["state_index"], g["states"]):
+        assert np.abs(states[k] - s).max() < TOL
+    # known answers of the reference at t = 40
+    assert abs(obs[-1, 0].real - 0.14233213) < 1e-8
+    assert abs(obs[-1, 1].real - 0.61325822) < 1e-8
+
+
+def test_jc16_inputs_match_generator(golden):
+    g = golden("jc16")
+    jc = W.jaynes_cummings()
+    assert np.array_equal(jc["H"], g["H"])
+    assert np.array_equal(np.stack(jc["c_ops"]), g["c_ops"])
+
+
+def test_gue64_fast(golden):
+    g = golden("gue64")
+    rho = O.fast_lindblad(g["H"], g["rho0"], list(g["c_ops"]), Nt=int(g["nt"]), dt=float(g["dt"]))
+    assert np.abs(rho - g["rho"]).max() < TOL
+
+
+def test_gue256_fast(golden):
+    g = golden("gue256")
+    w = W.gue_instance(N=256, K=4, seed=2)
+    if _digest(w["H"], *w["c_ops"], w["rho0"]) != str(g["digest"]):
+        pytest.skip("numpy's generator stream differs from the fixture's")
+    rho = O.fast_lindblad(w["H"], w["rho0"], w["c_ops"], Nt=int(g["nt"]), dt=float(g["dt"]))
+    assert np.abs(rho - g["rho"]).max() < TOL
+
+
+def test_exciton_correlation(golden):
+    g = golden("exciton")
+    ex = W.exciton_batch(indices=[int(i) for i in g["indices"]], nt=int(g["nt"]))
+    for i, n in enumerate(g["dims"]):
+        assert np.array_equal(ex["H"][i], g["H"][i, :n, :n])
+        c_dense = [np.diag(c) for c in ex["c_diag"][i]]
+        cor = O.correlation_2op_1t(ex["H"][i], ex["rho_g"][i], ex["mu"][i], ex["mu"][i], c_dense,
+                                   ex["dt"], ex["nt"])
+        assert np.abs(cor - g["cor"][i]).max() < TOL
+        cor_d = O.propagate_diag_correlation(ex["H"][i], ex["mu"][i], ex["rho_g"][i],
+                                             ex["c_diag"][i], ex["dt"], ex["nt"])
+        assert np.abs(cor_d - g["cor"][i]).max() < TOL
+
+
+def test_driven64(golden):
+    g = golden("driven64")
+    for b in range(2):
+        obs, states = O.lindblad_driven([g["H0"][b], [g["mu"][b], g["E"]]], g["rho0"][b],
+                                        list(g["L"][b]), [g["O"][b]], Nt=int(g["nt"]),
+                                        dt=float(g["dt"]))
+        assert np.abs(obs[:, 0] - g["observables"][b]).max() < TOL
+        assert np.abs(states[-1] - g["rho"][b]).max() < TOL
+
+
+def test_correlations_jc(golden):
+    g = golden("corr_jc")
+    jc = W.jaynes_cummings()
+    a, sm = g["a"], g["sm"]
+    ad, sp = a.conj().T, sm.conj().T
+    c2 = O.correlation_2op_1t(jc["H"], jc["rho0"], ad, a, jc["c_ops"], 0.02, 50)
+    assert np.abs(c2 - g["c2"]).max() < TOL
+    c3 = O.correlation_3op_1t(jc["H"], jc["rho0"], [ad, a @ ad, a], jc["c_ops"], 0.02, 50)
+    assert c3.shape == (51,) and np.abs(c3 - g["c3"]).max() < TOL
+    c4 = O.correlation_4op_1t(jc["H"], jc["rho0"], [ad, sp, sm, a], jc["c_ops"], 0.02, 50)
+    assert np.abs(c4 - g["c4"]).max() < TOL
+
+
+def test_rk4_matches_expm_liouvillian():
+    """Independent check: RK4 converges to expm(L t) rho0 (row-major vec)."""
+    from scipy.linalg import expm
+    jc = W.jaynes_cummings()
+    L = O.liouvillian_superop(jc["H"], jc["c_ops"])
+    _, states = O.lindblad(jc["H"], jc["rho0"], jc["c_ops"], [], Nt=200, dt=0.02)
+    ref = (expm(L * 4.0) @ jc["rho0"].ravel()).reshape(16, 16)
+    assert np.abs(states[-1] - ref).max() < 1e-10
+
+
+def test_rhs_diag_equals_dense():
+    rng = np.random.default_rng(0)
+    N, K = 7, 3
+    H = W.gue_matrix(rng, N)
+    cd = (rng.standard_normal((K, N)) + 1j * rng.standard_normal((K, N))) * 0.1
+    rho = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+    a = O.rhs(rho, H, [np.diag(c) for c in cd])
+    b = O.rhs_diag(rho, H, cd)
+    assert np.abs(a - b).max() < 1e-13
