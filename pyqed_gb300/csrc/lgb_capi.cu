@@ -39,6 +39,11 @@ int upload(lgb_plan* pl, T** dptr, const std::vector<T>& v) {
 void free_plan(lgb_plan* pl) {
   for (void* p : pl->allocations) cudaFree(p);
   pl->allocations.clear();
+  if (pl->side) cudaStreamDestroy(pl->side);
+  if (pl->ev_fork) cudaEventDestroy(pl->ev_fork);
+  if (pl->ev_join) cudaEventDestroy(pl->ev_join);
+  pl->side = nullptr;
+  pl->ev_fork = pl->ev_join = nullptr;
 }
 
 int validate(const lgb_problem_t* pr, const int32_t* dims) {
@@ -107,12 +112,18 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   pl->n_store = pr.store_every > 0 ? pr.nt / pr.store_every : 0;
   const int K = pr.n_cops;
   const bool dense = pr.cops_kind == LGB_COPS_DENSE;
-  int maxnp = 0;
+  const bool split = prec == LGB_PREC_TF32X3 || prec == LGB_PREC_BF16X3;
+  cudaDeviceGetAttribute(&pl->n_sm, cudaDevAttrMultiProcessorCount, pl->device);
+
+  // Tensor-core kernel: N <= 64 and no dense collapse operators (those keep
+  // the FP32 CTA kernel).  Its instances are padded to a multiple of 16.
+  std::vector<char> on_tc(n, 0);
+  for (int b = 0; b < n; ++b)
+    on_tc[b] = split && !dense && pl->dims[b] <= lgb::tc_max_dim() && pr.schedule != LGB_SCHED_GEMM;
   for (int b = 0; b < n; ++b) {
     const long long N = pl->dims[b];
-    const int NP = (int)((N + 3) / 4 * 4);
+    const int NP = on_tc[b] ? (int)((N + 15) / 16 * 16) : (int)((N + 3) / 4 * 4);
     pl->npad[b] = NP;
-    maxnp = std::max(maxnp, NP);
     pl->off[b] = pl->tot_off;
     pl->doff[b] = pl->tot_doff;
     pl->woff[b] = pl->tot_woff;
@@ -124,52 +135,69 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   }
 
   // ---- schedule ---------------------------------------------------------------
-  // The CTA-resident kernel needs A^T, X, X^T (+ dense-collapse scratch) in
-  // shared memory; anything larger goes to the grid-wide GEMM schedule.
+  // The CTA-resident kernels need the instance in shared memory; anything
+  // larger goes to the grid-wide GEMM schedule.
   int sched = pr.schedule;
-  bool cta_ok = maxnp <= lgb::cta_max_npad();
-  int smem = 0;
-  if (cta_ok) {
-    for (int b = 0; b < n; ++b) {
-      const long long ms = (long long)pl->npad[b] * (pl->npad[b] + pl->padc) * esz;
-      long long used = 3 * ms;
-      unsigned char pf = 0;
-      if (used > kSmemBudget) {
-        cta_ok = false;
-        break;
-      }
-      if (dense) {
-        if (used + K * ms <= kSmemBudget) {
-          used += K * ms;
-          pf |= 2;
-        }
-        if (used + K * ms <= kSmemBudget) {
-          used += K * ms;
-          pf |= 1;
-        }
-      }
-      pl->place[b] = pf;
-      smem = std::max<long long>(smem, used);
+  bool cta_ok = true;
+  int smem = 0, tc_smem = 0, tc_maxnp = 0;
+  for (int b = 0; b < n && cta_ok; ++b) {
+    if (on_tc[b]) {
+      tc_maxnp = std::max(tc_maxnp, pl->npad[b]);
+      continue;
     }
+    if (pl->npad[b] > lgb::cta_max_npad()) {
+      cta_ok = false;
+      break;
+    }
+    const long long ms = (long long)pl->npad[b] * (pl->npad[b] + pl->padc) * esz;
+    long long used = 3 * ms;
+    unsigned char pf = 0;
+    if (used > kSmemBudget) {
+      cta_ok = false;
+      break;
+    }
+    if (dense) {
+      if (used + K * ms <= kSmemBudget) {
+        used += K * ms;
+        pf |= 2;
+      }
+      if (used + K * ms <= kSmemBudget) {
+        used += K * ms;
+        pf |= 1;
+      }
+    }
+    pl->place[b] = pf;
+    smem = std::max<long long>(smem, used);
   }
+  if (tc_maxnp > 0) tc_smem = lgb::tc_smem_bytes(prec, tc_maxnp);
   if (sched == LGB_SCHED_AUTO) sched = cta_ok ? LGB_SCHED_CTA : LGB_SCHED_GEMM;
   if (sched == LGB_SCHED_CTA && !cta_ok) {
     delete pl;
     return LGB_ERR_UNSUPPORTED;
   }
-  if (sched == LGB_SCHED_GEMM || prec == LGB_PREC_TF32X3 || prec == LGB_PREC_BF16X3) {
+  if (sched == LGB_SCHED_GEMM) {
     delete pl;
     return LGB_ERR_UNSUPPORTED;
   }
   pl->schedule = sched;
   pl->smem_bytes = smem;
+  pl->tc_smem = tc_smem;
 
   // Largest instances first: with one CTA per instance the hardware block
-  // scheduler then performs longest-processing-time-first list scheduling.
-  pl->order.resize(n);
-  std::iota(pl->order.begin(), pl->order.end(), 0);
-  std::stable_sort(pl->order.begin(), pl->order.end(),
-                   [&](int a, int c) { return pl->npad[a] > pl->npad[c]; });
+  // scheduler then performs longest-processing-time-first list scheduling;
+  // the tensor-core kernel's work queue hands them out in the same order.
+  for (int b = 0; b < n; ++b) (on_tc[b] ? pl->tc_order : pl->order).push_back(b);
+  auto by_size = [&](int a, int c) { return pl->dims[a] > pl->dims[c]; };
+  std::stable_sort(pl->order.begin(), pl->order.end(), by_size);
+  std::stable_sort(pl->tc_order.begin(), pl->tc_order.end(), by_size);
+  if (!pl->order.empty() && !pl->tc_order.empty()) {
+    if (cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&pl->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      delete pl;
+      return LGB_ERR_CUDA;
+    }
+  }
 
   // ---- device buffers ---------------------------------------------------------
   s = LGB_OK;
@@ -177,6 +205,8 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   s = s ? s : upload(pl, &pl->d_dims, pl->dims);
   s = s ? s : upload(pl, &pl->d_npad, pl->npad);
   s = s ? s : upload(pl, &pl->d_order, pl->order);
+  s = s ? s : upload(pl, &pl->d_tc_order, pl->tc_order);
+  s = s ? s : dalloc(pl, &pl->d_queue, sizeof(int));
   s = s ? s : upload(pl, &pl->d_off, pl->off);
   s = s ? s : upload(pl, &pl->d_doff, pl->doff);
   s = s ? s : upload(pl, &pl->d_woff, pl->woff);
@@ -283,8 +313,34 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
   p.state_ws = plan->d_state;
   p.y_ws = plan->d_y;
   p.err = plan->d_err;
-  p.smem_bytes = plan->smem_bytes;
-  return cuda_status(lgb::launch_cta_rk4(p, pr.precision == LGB_PREC_FP64 ? 0 : 1, pr.n_inst, st));
+  const int n_cta = (int)plan->order.size();
+  const int n_tc = (int)plan->tc_order.size();
+  const int wprec = pr.precision == LGB_PREC_FP64 ? 0 : 1;
+  cudaError_t e = cudaSuccess;
+  if (n_cta > 0 && n_tc > 0) {
+    // the FP32 CTA kernel (large / dense-collapse instances) runs beside the
+    // tensor-core kernel on a forked stream
+    e = cudaEventRecord(plan->ev_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(plan->side, plan->ev_fork, 0);
+    p.order = plan->d_order;
+    p.smem_bytes = plan->smem_bytes;
+    if (e == cudaSuccess) e = lgb::launch_cta_rk4(p, wprec, n_cta, plan->side);
+    if (e == cudaSuccess) e = cudaEventRecord(plan->ev_join, plan->side);
+    p.smem_bytes = plan->tc_smem;
+    if (e == cudaSuccess)
+      e = lgb::launch_tc_rk4(p, pr.precision, plan->d_tc_order, n_tc, plan->d_queue,
+                             std::min(plan->n_sm, n_tc), st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, plan->ev_join, 0);
+  } else if (n_tc > 0) {
+    p.smem_bytes = plan->tc_smem;
+    e = lgb::launch_tc_rk4(p, pr.precision, plan->d_tc_order, n_tc, plan->d_queue,
+                           std::min(plan->n_sm, n_tc), st);
+  } else {
+    p.order = plan->d_order;
+    p.smem_bytes = plan->smem_bytes;
+    e = lgb::launch_cta_rk4(p, wprec, n_cta, st);
+  }
+  return cuda_status(e);
 }
 
 int lgb_plan_errors(lgb_plan_t plan, int32_t* flags_host) {
@@ -302,8 +358,8 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
   if (plan == nullptr || info == nullptr) return LGB_ERR_INVALID_ARG;
   info->schedule = plan->schedule;
   info->precision = plan->prob.precision;
-  info->smem_bytes = plan->smem_bytes;
-  info->launches_per_propagate = 1;
+  info->smem_bytes = std::max(plan->smem_bytes, plan->tc_smem);
+  info->launches_per_propagate = (plan->order.empty() ? 0 : 1) + (plan->tc_order.empty() ? 0 : 1);
   info->workspace_bytes = (int64_t)plan->ws_bytes;
   info->flops_per_step = plan->flops_per_step;
   return LGB_OK;

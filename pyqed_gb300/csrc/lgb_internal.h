@@ -16,6 +16,12 @@ int cta_max_npad();
 size_t cta_elem_bytes(int precision);
 cudaError_t launch_cta_rk4(const CtaParams& p, int precision, int n_blocks, cudaStream_t stream);
 
+// ---- tensor-core CTA-resident schedule (lgb_tc.cu) --------------------------
+int tc_max_dim();
+int tc_smem_bytes(int precision, int npad);
+cudaError_t launch_tc_rk4(const CtaParams& p, int precision, const int* order, int n_items,
+                          int* queue, int grid, cudaStream_t stream);
+
 // ---- operator preparation (lgb_setup.cu) -------------------------------------
 struct SetupParams {
   int n_inst, n_cops, cops_kind, n_eops, n_drive, padc;
@@ -47,7 +53,12 @@ struct lgb_plan {
   int padc = 2;
   bool ops_set = false;
   long long n_store = 0;
-  std::vector<int> dims, npad, order;
+  std::vector<int> dims, npad, order;      // order: CTA-kernel instances, largest first
+  std::vector<int> tc_order;               // tensor-core kernel instances, largest first
+  int tc_smem = 0;
+  int n_sm = 0;
+  cudaStream_t side = nullptr;             // second stream for the concurrent CTA kernel
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<long long> off, doff, woff, soff;
   std::vector<unsigned char> place;
   long long tot_off = 0, tot_doff = 0, tot_woff = 0;
@@ -58,6 +69,8 @@ struct lgb_plan {
   int* d_dims = nullptr;
   int* d_npad = nullptr;
   int* d_order = nullptr;
+  int* d_tc_order = nullptr;
+  int* d_queue = nullptr;
   long long* d_off = nullptr;
   long long* d_doff = nullptr;
   long long* d_woff = nullptr;

@@ -174,3 +174,81 @@ def test_correlation_two_time_intended_semantics():
     for k in range(4):
         ref = O.correlation_3op_1t(jc["H"], states[k], [ad, a @ ad, a], jc["c_ops"], 0.02, 6)
         assert np.abs(M[k] - ref).max() < TOL64
+
+
+# ---- split-precision tensor-core path --------------------------------------------
+
+@pytest.mark.parametrize("prec,tol", [("3xtf32", TOL32), ("3xbf16", 1e-3)])
+def test_split_exciton_golden(golden, prec, tol):
+    g = golden("exciton")
+    ex = W.exciton_batch(indices=[int(i) for i in g["indices"]], nt=int(g["nt"]))
+    cops = [[np.diag(c) for c in cd] for cd in ex["c_diag"]]
+    C = correlation_batch(ex["H"], cops, ex["rho_g"], ex["mu"], ex["mu"], ex["dt"], ex["nt"],
+                          precision=prec)
+    ref = g["cor"]
+    err = np.abs(C - ref).max() / np.abs(ref).max()
+    assert err < tol, err
+
+
+@pytest.mark.parametrize("prec,tol", [("3xtf32", TOL32), ("3xbf16", 1e-3)])
+def test_split_uneven_batch_vs_oracle(prec, tol):
+    # every padded size class of the tensor-core kernel (16/32/48/64) plus N=65
+    idx = list(range(40))
+    ex = W.exciton_batch(indices=idx, nt=25)
+    C = correlation_batch(ex["H"], [[np.diag(c) for c in cd] for cd in ex["c_diag"]],
+                          ex["rho_g"], ex["mu"], ex["mu"], ex["dt"], ex["nt"], precision=prec)
+    for i in range(len(idx)):
+        ref = O.propagate_diag_correlation(ex["H"][i], ex["mu"][i], ex["rho_g"][i],
+                                           ex["c_diag"][i], ex["dt"], ex["nt"])
+        assert np.abs(C[i] - ref).max() / np.abs(ref).max() < tol, (i, ex["dims"][i])
+
+
+def test_split_complex_dissipator_and_states():
+    """Complex diagonal collapse operators (D complex), no observables' t0 row,
+    states stored every 2 steps, Hermitian and non-Hermitian initial states."""
+    rng = np.random.default_rng(21)
+    dims = [5, 16, 17, 40, 64, 70]
+    H, cops, rho0 = [], [], []
+    for N in dims:
+        H.append(W.gue_matrix(rng, N))
+        cops.append([np.diag((rng.standard_normal(N) + 1j * rng.standard_normal(N)) * 0.1)
+                     for _ in range(3)])
+        r = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+        rho0.append(r / np.linalg.norm(r))
+    res = propagate_batch(H, cops, rho0, 0.02, 10, e_ops=[[h] for h in H], obs_t0=True,
+                          store_every=2, precision="3xtf32")
+    for b, N in enumerate(dims):
+        obs, states = O.lindblad(H[b], rho0[b], cops[b], [H[b]], Nt=10, dt=0.02)
+        assert np.abs(res["rho"][b] - states[-1]).max() < TOL32
+        assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < TOL32 * N
+        for k in range(5):
+            assert np.abs(res["states"][b][k] - states[2 * k + 1]).max() < TOL32
+
+
+def test_split_driven_diag_vs_oracle():
+    rng = np.random.default_rng(22)
+    dims = [8, 33, 64]
+    E = W.gp_pulse(15, 0.02, seed=9, amp=0.3)
+    H0 = [W.gue_matrix(rng, N) for N in dims]
+    mu = [W.gue_matrix(rng, N) for N in dims]
+    cops = [[np.diag(np.sqrt(0.02) * (np.arange(N) == k)) for k in range(2)] for N in dims]
+    rho0 = []
+    for N in dims:
+        psi = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        psi /= np.linalg.norm(psi)
+        rho0.append(np.outer(psi, psi.conj()))
+    res = propagate_batch(H0, cops, rho0, 0.02, 15, e_ops=[[m] for m in mu], obs_t0=False,
+                          precision="3xtf32", drive_ops=[[m] for m in mu], drive=E[None, :])
+    for b in range(len(dims)):
+        obs, states = O.lindblad_driven([H0[b], [mu[b], E]], rho0[b], cops[b], [mu[b]],
+                                        Nt=15, dt=0.02)
+        assert np.abs(res["rho"][b] - states[-1]).max() < TOL32
+        assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < TOL32 * 10
+
+
+def test_split_solver_run_matches_fp64():
+    jc = W.jaynes_cummings(nt=200)
+    sol = LindbladSolver(jc["H"], jc["c_ops"])
+    r64 = sol.run(jc["rho0"], dt=jc["dt"], Nt=200, e_ops=jc["e_ops"], precision="fp64")
+    r32 = sol.run(jc["rho0"], dt=jc["dt"], Nt=200, e_ops=jc["e_ops"], precision="3xtf32")
+    assert np.abs(r32.observables - r64.observables).max() < TOL32
