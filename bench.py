@@ -388,7 +388,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="exciton4096")
-    ap.add_argument("--precision", default=os.environ.get("LGB_BENCH_PRECISION", "fp32"))
+    ap.add_argument("--precision", default=os.environ.get("LGB_BENCH_PRECISION", "3xtf32"))
     ap.add_argument("--n-inst", type=int, default=None)
     ap.add_argument("--nt", type=int, default=None)
     ap.add_argument("--no-plain", action="store_true")

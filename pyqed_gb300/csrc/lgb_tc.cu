@@ -445,8 +445,8 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         for (int q = 0; q < 8; ++q) {
           const int jj = c0 + q;
           float R = v[q];
-          if (diag) R = fmaf(Dm[i * NPS + j0 + jj].x, xin[jj], R);
-          if (dcomplex) {
+          if (diag && i < NP) R = fmaf(Dm[i * NPS + j0 + jj].x, xin[jj], R);
+          if (dcomplex && i < NP) {
             const float di = Dm[i * NPS + j0 + jj].y;
             const float xo = sXc[((1 - comp) * 64 + i) * 64 + j0 + jj];
             R = fmaf(comp == 0 ? -di : di, xo, R);
