@@ -39,11 +39,14 @@ int upload(lgb_plan* pl, T** dptr, const std::vector<T>& v) {
 void free_plan(lgb_plan* pl) {
   for (void* p : pl->allocations) cudaFree(p);
   pl->allocations.clear();
-  if (pl->side) cudaStreamDestroy(pl->side);
+  for (int k = 0; k < 2; ++k) {
+    if (pl->side[k]) cudaStreamDestroy(pl->side[k]);
+    if (pl->ev_join[k]) cudaEventDestroy(pl->ev_join[k]);
+    pl->side[k] = nullptr;
+    pl->ev_join[k] = nullptr;
+  }
   if (pl->ev_fork) cudaEventDestroy(pl->ev_fork);
-  if (pl->ev_join) cudaEventDestroy(pl->ev_join);
-  pl->side = nullptr;
-  pl->ev_fork = pl->ev_join = nullptr;
+  pl->ev_fork = nullptr;
 }
 
 int validate(const lgb_problem_t* pr, const int32_t* dims) {
@@ -139,7 +142,8 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   // larger goes to the grid-wide GEMM schedule.
   int sched = pr.schedule;
   bool cta_ok = true;
-  int smem = 0, tc_smem = 0, tc_maxnp = 0;
+  int smem = 0, smem_w = 0, tc_smem = 0, tc_maxnp = 0;
+  std::vector<char> wide(n, 0);
   for (int b = 0; b < n && cta_ok; ++b) {
     if (on_tc[b]) {
       tc_maxnp = std::max(tc_maxnp, pl->npad[b]);
@@ -149,6 +153,8 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
       cta_ok = false;
       break;
     }
+    // FP32 instances with 64 < N <= 76 take the 384-thread single-round block
+    wide[b] = prec != LGB_PREC_FP64 && pl->npad[b] > 64 && pl->npad[b] <= lgb::cta_wide_max_npad();
     const long long ms = (long long)pl->npad[b] * (pl->npad[b] + pl->padc) * esz;
     long long used = 3 * ms;
     unsigned char pf = 0;
@@ -167,7 +173,11 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
       }
     }
     pl->place[b] = pf;
-    smem = std::max<long long>(smem, used);
+    if (wide[b]) {
+      smem_w = std::max<long long>(smem_w, used);
+    } else {
+      smem = std::max<long long>(smem, used);
+    }
   }
   if (tc_maxnp > 0) tc_smem = lgb::tc_smem_bytes(prec, tc_maxnp);
   if (sched == LGB_SCHED_AUTO) sched = cta_ok ? LGB_SCHED_CTA : LGB_SCHED_GEMM;
@@ -181,22 +191,28 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   }
   pl->schedule = sched;
   pl->smem_bytes = smem;
+  pl->smem_w = smem_w;
   pl->tc_smem = tc_smem;
 
   // Largest instances first: with one CTA per instance the hardware block
   // scheduler then performs longest-processing-time-first list scheduling;
   // the tensor-core kernel's work queue hands them out in the same order.
-  for (int b = 0; b < n; ++b) (on_tc[b] ? pl->tc_order : pl->order).push_back(b);
+  for (int b = 0; b < n; ++b) (on_tc[b] ? pl->tc_order : (wide[b] ? pl->order_w : pl->order)).push_back(b);
   auto by_size = [&](int a, int c) { return pl->dims[a] > pl->dims[c]; };
   std::stable_sort(pl->order.begin(), pl->order.end(), by_size);
+  std::stable_sort(pl->order_w.begin(), pl->order_w.end(), by_size);
   std::stable_sort(pl->tc_order.begin(), pl->tc_order.end(), by_size);
-  if (!pl->order.empty() && !pl->tc_order.empty()) {
-    if (cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&pl->ev_join, cudaEventDisableTiming) != cudaSuccess) {
-      delete pl;
-      return LGB_ERR_CUDA;
-    }
+  const int n_launch = (pl->order.empty() ? 0 : 1) + (pl->order_w.empty() ? 0 : 1) +
+                       (pl->tc_order.empty() ? 0 : 1);
+  bool ok = cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; k + 1 < n_launch && ok; ++k) {
+    ok = cudaStreamCreateWithFlags(&pl->side[k], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&pl->ev_join[k], cudaEventDisableTiming) == cudaSuccess;
+  }
+  if (!ok) {
+    free_plan(pl);
+    delete pl;
+    return LGB_ERR_CUDA;
   }
 
   // ---- device buffers ---------------------------------------------------------
@@ -205,6 +221,7 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   s = s ? s : upload(pl, &pl->d_dims, pl->dims);
   s = s ? s : upload(pl, &pl->d_npad, pl->npad);
   s = s ? s : upload(pl, &pl->d_order, pl->order);
+  s = s ? s : upload(pl, &pl->d_order_w, pl->order_w);
   s = s ? s : upload(pl, &pl->d_tc_order, pl->tc_order);
   s = s ? s : dalloc(pl, &pl->d_queue, sizeof(int));
   s = s ? s : upload(pl, &pl->d_off, pl->off);
@@ -218,6 +235,7 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   s = s ? s : dalloc(pl, &pl->d_Dm, pr.cops_kind == LGB_COPS_DIAG ? W * esz : 0);
   s = s ? s : dalloc(pl, &pl->d_Gt, (size_t)pr.n_drive * W * esz);
   s = s ? s : dalloc(pl, &pl->d_Ot, (size_t)pr.n_eops * W * sizeof(double2));
+  s = s ? s : dalloc(pl, &pl->d_OtF, prec == LGB_PREC_FP64 ? 0 : (size_t)pr.n_eops * W * sizeof(float2));
   s = s ? s : dalloc(pl, &pl->d_state, 2 * W * esz);
   s = s ? s : dalloc(pl, &pl->d_y, dense ? (size_t)K * W * esz : 0);
   s = s ? s : dalloc(pl, &pl->d_err, n * sizeof(int));
@@ -267,6 +285,7 @@ int lgb_plan_set_operators(lgb_plan_t plan, const double* H, const double* cops,
   sp.Dm = plan->d_Dm;
   sp.Gt = plan->d_Gt;
   sp.Ot = plan->d_Ot;
+  sp.OtF = plan->d_OtF;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   int s = cuda_status(lgb::launch_setup(sp, pr.precision == LGB_PREC_FP64 ? 0 : 1, st));
   if (s == LGB_OK) plan->ops_set = true;
@@ -305,6 +324,7 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
   p.Dm = plan->d_Dm;
   p.Gt = plan->d_Gt;
   p.Ot = plan->d_Ot;
+  p.OtF = plan->d_OtF;
   p.drive = drive_samples;
   p.rho0 = reinterpret_cast<const double2*>(rho0);
   p.obs_out = reinterpret_cast<double2*>(obs_out);
@@ -313,33 +333,42 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
   p.state_ws = plan->d_state;
   p.y_ws = plan->d_y;
   p.err = plan->d_err;
-  const int n_cta = (int)plan->order.size();
-  const int n_tc = (int)plan->tc_order.size();
+  // Up to three kernels (wide FP32 CTA, FP32 CTA, tensor-core) cover the
+  // batch; the first runs on the caller's stream, the others on forked
+  // streams joined back before return.
+  struct Launch {
+    int kind;  // 0 tensor core, 1 CTA, 2 wide CTA
+    int count;
+  };
+  Launch ls[3];
+  int nl = 0;
+  // The per-instance CTA kernels hold the longest single instances; they are
+  // launched first so that their blocks are resident from the start, and the
+  // persistent tensor-core blocks fill the remaining SMs from the work queue.
+  if (!plan->order_w.empty()) ls[nl++] = {2, (int)plan->order_w.size()};
+  if (!plan->order.empty()) ls[nl++] = {1, (int)plan->order.size()};
+  if (!plan->tc_order.empty()) ls[nl++] = {0, (int)plan->tc_order.size()};
   const int wprec = pr.precision == LGB_PREC_FP64 ? 0 : 1;
   cudaError_t e = cudaSuccess;
-  if (n_cta > 0 && n_tc > 0) {
-    // the FP32 CTA kernel (large / dense-collapse instances) runs beside the
-    // tensor-core kernel on a forked stream
+  if (nl > 1) {
     e = cudaEventRecord(plan->ev_fork, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(plan->side, plan->ev_fork, 0);
-    p.order = plan->d_order;
-    p.smem_bytes = plan->smem_bytes;
-    if (e == cudaSuccess) e = lgb::launch_cta_rk4(p, wprec, n_cta, plan->side);
-    if (e == cudaSuccess) e = cudaEventRecord(plan->ev_join, plan->side);
-    p.smem_bytes = plan->tc_smem;
-    if (e == cudaSuccess)
-      e = lgb::launch_tc_rk4(p, pr.precision, plan->d_tc_order, n_tc, plan->d_queue,
-                             std::min(plan->n_sm, n_tc), st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, plan->ev_join, 0);
-  } else if (n_tc > 0) {
-    p.smem_bytes = plan->tc_smem;
-    e = lgb::launch_tc_rk4(p, pr.precision, plan->d_tc_order, n_tc, plan->d_queue,
-                           std::min(plan->n_sm, n_tc), st);
-  } else {
-    p.order = plan->d_order;
-    p.smem_bytes = plan->smem_bytes;
-    e = lgb::launch_cta_rk4(p, wprec, n_cta, st);
+    for (int k = 1; k < nl && e == cudaSuccess; ++k)
+      e = cudaStreamWaitEvent(plan->side[k - 1], plan->ev_fork, 0);
   }
+  for (int k = 0; k < nl && e == cudaSuccess; ++k) {
+    cudaStream_t s_k = k == 0 ? st : plan->side[k - 1];
+    if (ls[k].kind == 0) {
+      p.smem_bytes = plan->tc_smem;
+      e = lgb::launch_tc_rk4(p, pr.precision, plan->d_tc_order, ls[k].count, plan->d_queue,
+                             std::min(plan->n_sm, ls[k].count), s_k);
+    } else {
+      p.order = ls[k].kind == 1 ? plan->d_order : plan->d_order_w;
+      p.smem_bytes = ls[k].kind == 1 ? plan->smem_bytes : plan->smem_w;
+      e = lgb::launch_cta_rk4(p, wprec, ls[k].count, s_k, ls[k].kind == 2);
+    }
+    if (e == cudaSuccess && k > 0) e = cudaEventRecord(plan->ev_join[k - 1], s_k);
+  }
+  for (int k = 1; k < nl && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, plan->ev_join[k - 1], 0);
   return cuda_status(e);
 }
 
@@ -358,8 +387,9 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
   if (plan == nullptr || info == nullptr) return LGB_ERR_INVALID_ARG;
   info->schedule = plan->schedule;
   info->precision = plan->prob.precision;
-  info->smem_bytes = std::max(plan->smem_bytes, plan->tc_smem);
-  info->launches_per_propagate = (plan->order.empty() ? 0 : 1) + (plan->tc_order.empty() ? 0 : 1);
+  info->smem_bytes = std::max(std::max(plan->smem_bytes, plan->smem_w), plan->tc_smem);
+  info->launches_per_propagate = (plan->order.empty() ? 0 : 1) + (plan->order_w.empty() ? 0 : 1) +
+                                 (plan->tc_order.empty() ? 0 : 1);
   info->workspace_bytes = (int64_t)plan->ws_bytes;
   info->flops_per_step = plan->flops_per_step;
   return LGB_OK;

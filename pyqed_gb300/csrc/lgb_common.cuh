@@ -72,6 +72,7 @@ struct CtaParams {
   const void* Dm;            // diagonal-c_ops dissipator D_ij, NP x NPS per instance
   const void* Gt;            // drive terms (i H_d)^T, n_drive x NP x NPS per instance
   const double2* Ot;         // observables transposed (FP64), n_eops x NP x NPS per instance
+  const float2* OtF;         // the same in FP32 (tensor-core kernel)
   const double* drive;       // drive samples
   const double2* rho0;       // packed initial states
   double2* obs_out;

@@ -24,8 +24,9 @@ namespace lgb {
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
+constexpr int kThreads = 256;      // default block: 4x4 tiles cover N <= 64 in one round
+constexpr int kThreadsWide = 384;  // wide block: one round for 64 < N <= 76
+constexpr int kMaxWarps = kThreadsWide / 32;
 constexpr int kMaxEops = 16;
 
 template <typename T2>
@@ -51,9 +52,10 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-template <typename T, int ROUNDS, bool SREG>
+template <typename T, int NT, int ROUNDS, bool SREG>
 __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsigned char* smem,
                                          double2 (*sRed)[kMaxEops], int* sFlag) {
+  constexpr int kWarps = NT / 32;
   using T2 = typename Cplx<T>::type;
   constexpr int PADC = 16 / (int)sizeof(T2);
   const int N = p.dims[b];
@@ -89,7 +91,7 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
     const T2* Ltg = reinterpret_cast<const T2*>(p.Lt) + (long long)K * wo;
     if (p.place[b] & 1) {
       T2* sLt = cursor;
-      for (int i = tid; i < K * MS; i += kThreads) sLt[i] = Ltg[i];
+      for (int i = tid; i < K * MS; i += NT) sLt[i] = Ltg[i];
       Lt = sLt;
     } else {
       Lt = Ltg;
@@ -106,7 +108,7 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
   bool act[ROUNDS];
 #pragma unroll
   for (int r = 0; r < ROUNDS; ++r) {
-    const int t = tid + r * kThreads;
+    const int t = tid + r * NT;
     act[r] = t < ntiles;
     ty[r] = act[r] ? t / nT : 0;
     tx[r] = act[r] ? t - ty[r] * nT : 0;
@@ -140,7 +142,7 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
     }
   }
   if (p.n_drive == 0) {
-    for (int i = tid; i < MS; i += kThreads) sAt[i] = At0[i];
+    for (int i = tid; i < MS; i += NT) sAt[i] = At0[i];
   }
 
   // FP64 observables Tr[O rho] and a finiteness check of the current state.
@@ -223,7 +225,7 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
       T f[4];
 #pragma unroll
       for (int d = 0; d < 4; ++d) f[d] = (d < p.n_drive) ? (T)drv[(long long)d * p.nt + step] : (T)0;
-      for (int i = tid; i < MS; i += kThreads) {
+      for (int i = tid; i < MS; i += NT) {
         T2 a = At0[i];
 #pragma unroll
         for (int d = 0; d < 4; ++d)
@@ -431,35 +433,51 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 1) cta_rk4_kernel(CtaParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double2 sRed[kWarps][kMaxEops];
-  __shared__ int sFlag[kWarps];
+  __shared__ double2 sRed[kThreads / 32][kMaxEops];
+  __shared__ int sFlag[kThreads / 32];
   const int b = p.order[blockIdx.x];
   const int NP = p.npad[b];
   if constexpr (std::is_same<T, float>::value) {
     if (NP <= 64) {
-      cta_body<T, 1, true>(p, b, smem, sRed, sFlag);
+      cta_body<T, kThreads, 1, true>(p, b, smem, sRed, sFlag);
     } else {
-      cta_body<T, 2, false>(p, b, smem, sRed, sFlag);
+      cta_body<T, kThreads, 2, false>(p, b, smem, sRed, sFlag);
     }
   } else {
     if (NP <= 64) {
-      cta_body<T, 1, false>(p, b, smem, sRed, sFlag);
+      cta_body<T, kThreads, 1, false>(p, b, smem, sRed, sFlag);
     } else {
-      cta_body<T, 2, false>(p, b, smem, sRed, sFlag);
+      cta_body<T, kThreads, 2, false>(p, b, smem, sRed, sFlag);
     }
   }
+}
+
+// FP32, 64 < N <= 76: one 4x4 tile per thread, state in registers.
+__global__ void __launch_bounds__(kThreadsWide, 1) cta_rk4_wide_kernel(CtaParams p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double2 sRed[kThreadsWide / 32][kMaxEops];
+  __shared__ int sFlag[kThreadsWide / 32];
+  const int b = p.order[blockIdx.x];
+  cta_body<float, kThreadsWide, 1, true>(p, b, smem, sRed, sFlag);
 }
 
 }  // namespace
 
 int cta_max_npad() { return 88; }
+int cta_wide_max_npad() { return 76; }
 
 size_t cta_elem_bytes(int precision) { return precision == 0 ? sizeof(double2) : sizeof(float2); }
 
-cudaError_t launch_cta_rk4(const CtaParams& p, int precision, int n_blocks, cudaStream_t stream) {
+cudaError_t launch_cta_rk4(const CtaParams& p, int precision, int n_blocks, cudaStream_t stream,
+                           bool wide) {
   if (n_blocks <= 0) return cudaSuccess;
   cudaError_t e;
-  if (precision == 0) {
+  if (wide) {
+    e = cudaFuncSetAttribute(cta_rk4_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             p.smem_bytes);
+    if (e != cudaSuccess) return e;
+    cta_rk4_wide_kernel<<<n_blocks, kThreadsWide, p.smem_bytes, stream>>>(p);
+  } else if (precision == 0) {
     e = cudaFuncSetAttribute(cta_rk4_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              p.smem_bytes);
     if (e != cudaSuccess) return e;

@@ -13,8 +13,10 @@ namespace lgb {
 
 // ---- CTA-resident schedule (lgb_cta.cu) -------------------------------------
 int cta_max_npad();
+int cta_wide_max_npad();
 size_t cta_elem_bytes(int precision);
-cudaError_t launch_cta_rk4(const CtaParams& p, int precision, int n_blocks, cudaStream_t stream);
+cudaError_t launch_cta_rk4(const CtaParams& p, int precision, int n_blocks, cudaStream_t stream,
+                           bool wide);
 
 // ---- tensor-core CTA-resident schedule (lgb_tc.cu) --------------------------
 int tc_max_dim();
@@ -40,6 +42,7 @@ struct SetupParams {
   void* Dm;
   void* Gt;
   double2* Ot;
+  float2* OtF;  // FP32 copy of Ot (FP32-working plans only)
 };
 cudaError_t launch_setup(const SetupParams& p, int precision, cudaStream_t stream);
 
@@ -54,11 +57,14 @@ struct lgb_plan {
   bool ops_set = false;
   long long n_store = 0;
   std::vector<int> dims, npad, order;      // order: CTA-kernel instances, largest first
+  std::vector<int> order_w;                // 384-thread FP32 CTA-kernel instances (64 < N <= 76)
   std::vector<int> tc_order;               // tensor-core kernel instances, largest first
   int tc_smem = 0;
+  int smem_w = 0;
   int n_sm = 0;
-  cudaStream_t side = nullptr;             // second stream for the concurrent CTA kernel
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t side[2] = {nullptr, nullptr};  // streams for kernels that run beside the first
+  cudaEvent_t ev_fork = nullptr;
+  cudaEvent_t ev_join[2] = {nullptr, nullptr};
   std::vector<long long> off, doff, woff, soff;
   std::vector<unsigned char> place;
   long long tot_off = 0, tot_doff = 0, tot_woff = 0;
@@ -69,6 +75,7 @@ struct lgb_plan {
   int* d_dims = nullptr;
   int* d_npad = nullptr;
   int* d_order = nullptr;
+  int* d_order_w = nullptr;
   int* d_tc_order = nullptr;
   int* d_queue = nullptr;
   long long* d_off = nullptr;
@@ -82,6 +89,7 @@ struct lgb_plan {
   void* d_Dm = nullptr;
   void* d_Gt = nullptr;
   double2* d_Ot = nullptr;
+  float2* d_OtF = nullptr;
   void* d_state = nullptr;
   void* d_y = nullptr;
   int* d_err = nullptr;

@@ -112,6 +112,8 @@ __global__ void setup_kernel(SetupParams p) {
       double2 v = make_double2(0.0, 0.0);
       if (in) v = p.eops[(long long)p.n_eops * o + e * NN + (long long)q * N + r];
       p.Ot[(long long)p.n_eops * wo + e * MS + idx] = v;
+      if (p.OtF != nullptr)
+        p.OtF[(long long)p.n_eops * wo + e * MS + idx] = make_float2((float)v.x, (float)v.y);
     }
   }
 }

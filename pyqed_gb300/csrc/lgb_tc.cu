@@ -18,8 +18,8 @@
 // lo*hi, correction terms first) with FP32 accumulation; the 64-bit
 // algorithmic count is 64 N^3 real flops per instance-step.
 //
-// Each of the 256 threads owns one TMEM lane (one component of one row) and
-// half of its columns; it keeps rho, the RK4 sum, a Kahan compensation term
+// Each of the 512 threads owns a quarter of one TMEM lane's columns (a lane
+// is one component of one row); it keeps rho, the RK4 sum, a Kahan compensation term
 // and the stage input in registers, performs the RK4 stage combination
 // (pyqed/phys.py:1051-1064) with a Kahan-compensated final update, splits the
 // next stage input into hi/lo and writes it into SX.  Observables Tr[O rho]
@@ -37,7 +37,7 @@ namespace {
 
 using namespace umma;
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxEops = 16;
 
@@ -72,30 +72,6 @@ __device__ __forceinline__ uint32_t toff(int r, int c, uint32_t sbo) {
          (uint32_t)(c % EPC) * Elem<BF16>::kSize;
 }
 
-// Store 4 (TF32) or 8 (BF16) consecutive columns of one row (16 bytes).
-template <bool BF16, int W>
-__device__ __forceinline__ void st16(unsigned char* base, const float* v) {
-  if constexpr (!BF16) {
-    *reinterpret_cast<float4*>(base) = make_float4(v[0], v[1], v[2], v[3]);
-  } else {
-    __nv_bfloat162 p0 = __floats2bfloat162_rn(v[0], v[1]);
-    __nv_bfloat162 p1 = __floats2bfloat162_rn(v[2], v[3]);
-    __nv_bfloat162 p2 = __floats2bfloat162_rn(v[4], v[5]);
-    __nv_bfloat162 p3 = __floats2bfloat162_rn(v[6], v[7]);
-    uint4 u;
-    u.x = *reinterpret_cast<uint32_t*>(&p0);
-    u.y = *reinterpret_cast<uint32_t*>(&p1);
-    u.z = *reinterpret_cast<uint32_t*>(&p2);
-    u.w = *reinterpret_cast<uint32_t*>(&p3);
-    *reinterpret_cast<uint4*>(base) = u;
-  }
-}
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 struct TcShared {
   uint64_t mbar;
@@ -151,13 +127,17 @@ __device__ __forceinline__ void group_ax(uint32_t d, uint32_t sa, uint32_t sxt, 
   constexpr uint32_t id = idesc(Elem<BF16>::kFmt, 128, NP, false, false);
   const uint64_t da = sdesc(sa, G::LBO_S, G::SBO_S);
   const uint64_t db = sdesc(sxt, G::LBO_T, G::SBO_T);
+  // the K loop is unrolled (descriptors = chunk base + compile-time constant,
+  // no dependent address arithmetic between MMAs); the chunk loop is not, to
+  // bound register pressure
 #pragma unroll 1
   for (int chunk = 0; chunk < 2; ++chunk) {
     const uint32_t a_off = (chunk == 0 ? 8u : 0u) * G::SBO_S;       // [Ar;Ai] or [-Ai;Ar]
     const uint32_t b_off = (uint32_t)chunk * (NP / 8) * G::SBO_T;    // Xr^T or Xi^T
-#pragma unroll 1
+    const uint64_t ca = dadd(da, a_off), cb = dadd(db, b_off);
+#pragma unroll
     for (int s = 0; s < G::KS; ++s) {
-      mma<BF16>(d, dadd(da, a_off + s * G::KSTEP_S), dadd(db, b_off + s * G::KSTEP_T), id, acc);
+      mma<BF16>(d, dadd(ca, s * G::KSTEP_S), dadd(cb, s * G::KSTEP_T), id, acc);
       acc = 1;
     }
   }
@@ -174,9 +154,10 @@ __device__ __forceinline__ void group_xa(uint32_t d, uint32_t sx, uint32_t sa, u
   for (int chunk = 0; chunk < 2; ++chunk) {
     const uint32_t a_off = (chunk == 0 ? 0u : 8u) * G::SBO_S;        // [Xr;Xi] or [Xi;-Xr]
     const uint32_t b_off = (chunk == 0 ? 8u : 16u) * G::SBO_S;       // Ar or Ai block
-#pragma unroll 1
+    const uint64_t ca = dadd(da, a_off), cb = dadd(db, b_off);
+#pragma unroll
     for (int s = 0; s < G::KS; ++s) {
-      mma<BF16>(d, dadd(da, a_off + s * G::KSTEP_S), dadd(db, b_off + s * G::KSTEP_S), id, acc);
+      mma<BF16>(d, dadd(ca, s * G::KSTEP_S), dadd(cb, s * G::KSTEP_S), id, acc);
       acc = 1;
     }
   }
@@ -188,6 +169,38 @@ __device__ __forceinline__ void sync_for_mma() {
   __syncthreads();
 }
 
+// Store 4 consecutive columns of one operand row (16 bytes TF32, 8 bytes BF16).
+template <bool BF16>
+__device__ __forceinline__ void st4(unsigned char* base, const float* v) {
+  if constexpr (!BF16) {
+    *reinterpret_cast<float4*>(base) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    __nv_bfloat162 p0 = __floats2bfloat162_rn(v[0], v[1]);
+    __nv_bfloat162 p1 = __floats2bfloat162_rn(v[2], v[3]);
+    uint2 u;
+    u.x = *reinterpret_cast<uint32_t*>(&p0);
+    u.y = *reinterpret_cast<uint32_t*>(&p1);
+    *reinterpret_cast<uint2*>(base) = u;
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float* v) {
+  if constexpr (W == 4) {
+    tmem_ld4(taddr, v);
+  } else if constexpr (W == 8) {
+    tmem_ld8(taddr, v);
+  } else if constexpr (W == 12) {
+    tmem_ld8(taddr, v);
+    tmem_ld4(taddr + 8, v + 8);
+  } else {
+    tmem_ld16(taddr, v);
+  }
+}
+
+// One instance, all Nt steps.  Thread mapping: warp w reads TMEM lane quarter
+// (w & 3) and owns columns [(w >> 2) NP/4, (w >> 2 + 1) NP/4) of its lane;
+// lane l holds component l / 64 (0 real, 1 imaginary) of row l % 64.
 template <bool BF16, int NP>
 __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem, TcShared& sh,
                             uint32_t& phase, bool& alive) {
@@ -195,15 +208,15 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   using G = Geo<BF16, NP>;
   using ET = typename El::T;
   constexpr int EPC = G::EPC;
-  constexpr int NPH = NP / 2;
-  constexpr int kGroups = NPH / EPC;          // 16-byte groups per thread row segment
+  constexpr int NPQ = NP / 4;                 // columns per thread
+  constexpr int NG = NPQ / 4;                 // groups of 4 columns
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, half = warp >> 2;
+  const int quarter = warp & 3, cg = warp >> 2;
   const int l = quarter * 32 + lane;  // TMEM lane
   const int comp = l >> 6;            // 0: real part, 1: imaginary part
   const int i = l & 63;               // row
-  const int j0 = half * NPH;          // first owned column
+  const int j0 = cg * NPQ;            // first owned column
   const int N = p.dims[b];
   const int NPS = NP + 2;             // row stride of the FP32 working matrices
   const long long wo = p.woff[b];
@@ -224,7 +237,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const float2* At0 = reinterpret_cast<const float2*>(p.At) + wo;
   const float2* Gt = reinterpret_cast<const float2*>(p.Gt) + (long long)p.n_drive * wo;
   const float2* Dm = reinterpret_cast<const float2*>(p.Dm) + wo;
-  const double2* Ot = p.Ot + (long long)E * wo;
+  const float2* OtF = p.OtF + (long long)E * wo;
   const uint32_t taddr = sh.tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)j0;
 
   // ---- A stack: SA = [-Ai ; Ar ; Ai] (hi / lo), rebuilt per step when driven --
@@ -259,24 +272,24 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
 
   // ---- X operands: SX = [Xr ; Xi ; -Xr] rows, SXT = [Xr^T ; Xi^T] -------------
   // level: 0 = hi part, 1 = lo part of the split of x.
+  const int xrow = comp == 0 ? i : 64 + i;
   auto write_x = [&](const float* x, int level, unsigned char* SX, unsigned char* SXT) {
-    const int r = comp == 0 ? i : 64 + i;
 #pragma unroll
-    for (int g = 0; g < kGroups; ++g) {
-      float v[EPC], nv[EPC];
+    for (int g = 0; g < NG; ++g) {
+      float v[4], nv[4];
 #pragma unroll
-      for (int e = 0; e < EPC; ++e) {
+      for (int e = 0; e < 4; ++e) {
         float h, lo;
-        El::split(x[g * EPC + e], h, lo);
+        El::split(x[g * 4 + e], h, lo);
         v[e] = level == 0 ? h : lo;
         nv[e] = -v[e];
       }
-      const int c = j0 + g * EPC;
-      st16<BF16, EPC>(SX + toff<BF16>(r, c, G::SBO_S), v);
-      if (comp == 0) st16<BF16, EPC>(SX + toff<BF16>(128 + i, c, G::SBO_S), nv);
+      const int c = j0 + g * 4;
+      st4<BF16>(SX + toff<BF16>(xrow, c, G::SBO_S), v);
+      if (comp == 0) st4<BF16>(SX + toff<BF16>(128 + i, c, G::SBO_S), nv);
       if (i < NP) {
 #pragma unroll
-        for (int e = 0; e < EPC; ++e) {
+        for (int e = 0; e < 4; ++e) {
           const int rt = comp * NP + c + e;  // row of X^T (= column of X)
           const uint32_t o = (uint32_t)(rt >> 3) * G::SBO_T + (uint32_t)(i / EPC) * G::LBO_T +
                              (uint32_t)(rt & 7) * 16u + (uint32_t)(i % EPC) * El::kSize;
@@ -286,31 +299,49 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     }
   };
 
-  // ---- FP64 observables + finiteness of rho (block reduction) -----------------
+  // ---- observables Tr[O rho]: FP32 partials per thread and warp (pairwise
+  // shuffle tree), FP64 across warps.  A per-thread mask skips the zero
+  // entries of O (sparse observables such as a transition dipole).
+  uint32_t omask = 0;  // bit e*NPQ+jj (E * NPQ <= 32 bits used)
+  const bool use_mask = E * NPQ <= 32;
+  if (use_mask && i < N) {
+    for (int e = 0; e < E; ++e) {
+      const float2* o = OtF + (long long)e * NP * NPS + (long long)i * NPS + j0;
+#pragma unroll
+      for (int jj = 0; jj < NPQ; ++jj) {
+        const float2 ov = o[jj];
+        if (ov.x != 0.f || ov.y != 0.f) omask |= 1u << (e * NPQ + jj);
+      }
+    }
+  }
   auto reduce_state = [&](const float* rho, int row) -> bool {
     bool fin = true;
 #pragma unroll
-    for (int jj = 0; jj < NPH; ++jj) fin = fin && isfinite(rho[jj]);
+    for (int jj = 0; jj < NPQ; ++jj) fin = fin && isfinite(rho[jj]);
     for (int e = 0; e < E; ++e) {
-      double sx = 0.0, sy = 0.0;
-      if (i < N) {
-        const double2* o = Ot + (long long)e * NP * NPS + (long long)i * NPS + j0;
+      float fx = 0.f, fy = 0.f;
+      const uint32_t m = use_mask ? (omask >> (e * NPQ)) : 0xffffffffu;
+      if (i < N && (m & ((NPQ >= 32) ? 0xffffffffu : ((1u << NPQ) - 1u))) != 0u) {
+        const float2* o = OtF + (long long)e * NP * NPS + (long long)i * NPS + j0;
 #pragma unroll
-        for (int jj = 0; jj < NPH; ++jj) {
-          const double2 ov = o[jj];  // O[j][i]
-          const double x = (double)rho[jj];
+        for (int jj = 0; jj < NPQ; ++jj) {
+          if (!(m & (1u << jj))) continue;
+          const float2 ov = o[jj];  // O[j][i]
           if (comp == 0) {
-            sx += ov.x * x;
-            sy += ov.y * x;
+            fx = fmaf(ov.x, rho[jj], fx);
+            fy = fmaf(ov.y, rho[jj], fy);
           } else {
-            sx -= ov.y * x;
-            sy += ov.x * x;
+            fx = fmaf(-ov.y, rho[jj], fx);
+            fy = fmaf(ov.x, rho[jj], fy);
           }
         }
       }
-      sx = warp_sum(sx);
-      sy = warp_sum(sy);
-      if (lane == 0) sh.red[warp][e] = make_double2(sx, sy);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+      }
+      if (lane == 0) sh.red[warp][e] = make_double2((double)fx, (double)fy);
     }
     const unsigned bad = __ballot_sync(0xffffffffu, !fin);
     if (lane == 0) sh.flag[warp] = bad != 0u;
@@ -319,14 +350,14 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) anybad = anybad || sh.flag[w];
     if (tid < E && p.obs_out != nullptr) {
-      double2 s = make_double2(0.0, 0.0);
+      double2 sacc = make_double2(0.0, 0.0);
 #pragma unroll
       for (int w = 0; w < kWarps; ++w) {
-        s.x += sh.red[w][tid].x;
-        s.y += sh.red[w][tid].y;
+        sacc.x += sh.red[w][tid].x;
+        sacc.y += sh.red[w][tid].y;
       }
       const long long nrows = (long long)p.nt + p.obs_t0;
-      p.obs_out[((long long)b * nrows + row) * E + tid] = s;
+      p.obs_out[((long long)b * nrows + row) * E + tid] = sacc;
     }
     return anybad;
   };
@@ -345,11 +376,11 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   };
 
   // ---- state -------------------------------------------------------------------
-  float rho[NPH], racc[NPH], kc[NPH], xin[NPH];
+  float rho[NPQ], racc[NPQ], kc[NPQ], xin[NPQ];
   {
     const double2* r0 = p.rho0 + p.off[b];
 #pragma unroll
-    for (int jj = 0; jj < NPH; ++jj) {
+    for (int jj = 0; jj < NPQ; ++jj) {
       const int j = j0 + jj;
       double v = 0.0;
       if (i < N && j < N) {
@@ -362,17 +393,28 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       kc[jj] = 0.f;
     }
   }
-  // A complex dissipator matrix couples the real and imaginary lanes; those
-  // instances exchange the stage input through shared memory.
-  bool dc = false;
+
+  // Dissipator D o X of diagonal collapse operators.  Pure-dephasing type
+  // (D diagonal and real) keeps D_ii in a register; a general D is read from
+  // the working copy; a complex D couples the real and imaginary lanes, which
+  // then exchange the stage input through shared memory.
+  bool off = false, dc = false;
   if (diag && i < N) {
 #pragma unroll
-    for (int jj = 0; jj < NPH; ++jj) dc = dc || (Dm[i * NPS + j0 + jj].y != 0.f);
+    for (int jj = 0; jj < NPQ; ++jj) {
+      const float2 d = Dm[i * NPS + j0 + jj];
+      off = off || ((j0 + jj != i) && (d.x != 0.f || d.y != 0.f));
+      dc = dc || (d.y != 0.f);
+    }
   }
+  const bool dgeneral = __syncthreads_or(off) != 0;
   const bool dcomplex = __syncthreads_or(dc) != 0;
+  const bool dfast = diag && !dgeneral && !dcomplex;
+  const int dpos = (i >= j0 && i < j0 + NPQ) ? i - j0 : -1;
+  const float dd = (dfast && dpos >= 0 && i < N) ? Dm[i * NPS + i].x : 0.f;
   auto publish_x = [&]() {
 #pragma unroll
-    for (int jj = 0; jj < NPH; ++jj) sXc[(comp * 64 + i) * 64 + j0 + jj] = xin[jj];
+    for (int jj = 0; jj < NPQ; ++jj) sXc[(comp * 64 + i) * 64 + j0 + jj] = xin[jj];
   };
   if (dcomplex) publish_x();
   if (p.n_drive == 0) build_sa(nullptr);
@@ -434,37 +476,45 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         if (!wait_mma()) break;
       }
       fence_after_sync();
-      const float cst = (stage == 2) ? dt : half_dt;
-      // epilogue in chunks of 8 columns: TMEM -> registers -> RK4 stage combination
-#pragma unroll
-      for (int c0 = 0; c0 < NPH; c0 += 8) {
-        float v[8];
-        tmem_ld8(taddr + c0, v);
-        tmem_wait_ld();
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int jj = c0 + q;
-          float R = v[q];
-          if (diag && i < NP) R = fmaf(Dm[i * NPS + j0 + jj].x, xin[jj], R);
-          if (dcomplex && i < NP) {
-            const float di = Dm[i * NPS + j0 + jj].y;
+      float v[NPQ];
+      tmem_ld_cols<NPQ>(taddr, v);
+      tmem_wait_ld();
+      // RHS element R = v + (D o X); stages 0-2 form the RK4 sum and the next
+      // stage input, stage 3 applies the Kahan-compensated update
+      auto rhs = [&](int jj) -> float {
+        float R = v[jj];
+        if (dfast) {
+          R = (jj == dpos) ? fmaf(dd, xin[jj], R) : R;
+        } else if (diag && i < NP) {
+          const float2 d = Dm[i * NPS + j0 + jj];
+          R = fmaf(d.x, xin[jj], R);
+          if (dcomplex) {
             const float xo = sXc[((1 - comp) * 64 + i) * 64 + j0 + jj];
-            R = fmaf(comp == 0 ? -di : di, xo, R);
+            R = fmaf(comp == 0 ? -d.y : d.y, xo, R);
           }
-          if (stage == 0) {
-            racc[jj] = R;
-            xin[jj] = fmaf(cst, R, rho[jj]);
-          } else if (stage < 3) {
-            racc[jj] = fmaf(2.f, R, racc[jj]);
-            xin[jj] = fmaf(cst, R, rho[jj]);
-          } else {
-            // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4)
-            const float y = fmaf(sixth_dt, racc[jj] + R, -kc[jj]);
-            const float t = rho[jj] + y;
-            kc[jj] = (t - rho[jj]) - y;
-            rho[jj] = t;
-            xin[jj] = t;
-          }
+        }
+        return R;
+      };
+      if (stage < 3) {
+        const float cst = (stage == 2) ? dt : half_dt;
+        const float keep = (stage == 0) ? 0.f : 1.f;
+        const float w = (stage == 0) ? 1.f : 2.f;
+#pragma unroll
+        for (int jj = 0; jj < NPQ; ++jj) {
+          const float R = rhs(jj);
+          racc[jj] = fmaf(w, R, keep * racc[jj]);
+          xin[jj] = fmaf(cst, R, rho[jj]);
+        }
+      } else {
+#pragma unroll
+        for (int jj = 0; jj < NPQ; ++jj) {
+          const float R = rhs(jj);
+          // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4)
+          const float y = fmaf(sixth_dt, racc[jj] + R, -kc[jj]);
+          const float t = rho[jj] + y;
+          kc[jj] = (t - rho[jj]) - y;
+          rho[jj] = t;
+          xin[jj] = t;
         }
       }
       if (dcomplex) {
@@ -483,7 +533,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       const long long si = (step + 1) / p.store_every - 1;
       double2* dst = p.states_out + p.soff[b] + si * (long long)N * N;
 #pragma unroll
-      for (int jj = 0; jj < NPH; ++jj) {
+      for (int jj = 0; jj < NPQ; ++jj) {
         const int j = j0 + jj;
         if (j < N) reinterpret_cast<double*>(dst + (long long)i * N + j)[comp] = (double)rho[jj];
       }
@@ -493,7 +543,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   if (alive && p.rho_out != nullptr && i < N) {
     double2* dst = p.rho_out + p.off[b];
 #pragma unroll
-    for (int jj = 0; jj < NPH; ++jj) {
+    for (int jj = 0; jj < NPQ; ++jj) {
       const int j = j0 + jj;
       if (j < N) reinterpret_cast<double*>(dst + (long long)i * N + j)[comp] = (double)rho[jj];
     }
