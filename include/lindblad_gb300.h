@@ -42,7 +42,8 @@ enum {
   LGB_ERR_NONFINITE = 4,    /* some instance's state became NaN/Inf              */
   LGB_ERR_TIMEOUT = 5,      /* a bounded device wait gave up                     */
   LGB_ERR_NO_DEVICE = 6,    /* no CUDA device visible                            */
-  LGB_ERR_STATE = 7         /* call order violated (e.g. propagate before set)   */
+  LGB_ERR_STATE = 7,        /* call order violated (e.g. propagate before set)   */
+  LGB_ERR_TOO_LARGE = 8     /* request exceeds the no-allocation scratch limits  */
 };
 
 /* ---- precisions ------------------------------------------------------------ */
@@ -145,6 +146,43 @@ typedef struct {
 } lgb_plan_info_t;
 
 int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
+
+/* ---- propagation without device allocation ---------------------------------
+ * No counterpart in the reference: pyqed is pure Python and never manages
+ * device memory.
+ *
+ * For callers that cannot call cudaMalloc -- a process whose device memory
+ * was handed to another allocator up front (a framework's caching allocator,
+ * a fixed arena in a serving process), or code issuing work while a stream
+ * is being captured into a CUDA graph, where allocation is not allowed.
+ * It propagates ONE instance in complex128 (the same FP64 kernel as
+ * lgb_plan_propagate with LGB_PREC_FP64) and keeps every working buffer in a
+ * fixed array compiled into the library (about 1.1 MB, held on every device
+ * that loads the library until the process exits); it never allocates.
+ *
+ *   H          N x N Hamiltonian (device, complex128)
+ *   cops       n_cops collapse operators, dense (N x N each) or diagonals
+ *              (N each) per cops_kind; NULL when n_cops == 0
+ *   eops       n_eops observables (N x N each); NULL when n_eops == 0
+ *   rho0       initial state (N x N)
+ *   obs_out    [nt + obs_t0][n_eops] complex128, or NULL
+ *   rho_out    final state (N x N), or NULL
+ *   status_out one int32 on the device receiving LGB_OK or LGB_ERR_NONFINITE
+ *              for this propagation, or NULL
+ * Limits: N <= LGB_NOALLOC_MAX_DIM, n_cops <= LGB_NOALLOC_MAX_COPS,
+ * n_eops <= LGB_NOALLOC_MAX_EOPS; larger requests return LGB_ERR_TOO_LARGE.
+ * The first call on a device looks up the array's device address (once per
+ * device); make that first call before any stream capture begins.  All calls
+ * share the one array, so calls that overlap on the GPU (different streams,
+ * or different host threads on the same device) race: serialise them.
+ * Asynchronous on `stream`. */
+#define LGB_NOALLOC_MAX_DIM 64
+#define LGB_NOALLOC_MAX_COPS 4
+#define LGB_NOALLOC_MAX_EOPS 4
+int lgb_propagate_noalloc(const double* H, int32_t n, const double* cops, int32_t n_cops,
+                          int32_t cops_kind, const double* eops, int32_t n_eops,
+                          const double* rho0, int32_t nt, double dt, int32_t obs_t0,
+                          double* obs_out, double* rho_out, int32_t* status_out, void* stream);
 
 #ifdef __cplusplus
 }

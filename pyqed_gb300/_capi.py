@@ -23,6 +23,8 @@ LGB_ERR_NONFINITE = 4
 LGB_ERR_TIMEOUT = 5
 LGB_ERR_NO_DEVICE = 6
 LGB_ERR_STATE = 7
+LGB_ERR_TOO_LARGE = 8
+NOALLOC_MAX_DIM, NOALLOC_MAX_COPS, NOALLOC_MAX_EOPS = 64, 4, 4
 
 # precisions
 PREC = {"fp64": 0, "fp32": 1, "3xtf32": 2, "3xbf16": 3}
@@ -37,6 +39,7 @@ SCHED_NAME = {v: k for k, v in SCHED.items()}
 EXPORTS = [
     "lgb_get_version", "lgb_status_string", "lgb_plan_create", "lgb_plan_destroy",
     "lgb_plan_set_operators", "lgb_plan_propagate", "lgb_plan_errors", "lgb_plan_get_info",
+    "lgb_propagate_noalloc",
 ]
 
 
@@ -104,6 +107,9 @@ def lib():
     L.lgb_plan_errors.argtypes = [vp, ctypes.POINTER(i32)]
     L.lgb_plan_get_info.restype = ctypes.c_int
     L.lgb_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+    L.lgb_propagate_noalloc.restype = ctypes.c_int
+    L.lgb_propagate_noalloc.argtypes = [dp, i32, dp, i32, i32, dp, i32, dp, i32, ctypes.c_double,
+                                        i32, dp, dp, dp, vp]
     _lib = L
     return L
 

@@ -81,6 +81,7 @@ const char* lgb_status_string(int status) {
     case LGB_ERR_TIMEOUT: return "bounded device wait timed out";
     case LGB_ERR_NO_DEVICE: return "no CUDA device";
     case LGB_ERR_STATE: return "call order violated";
+    case LGB_ERR_TOO_LARGE: return "size exceeds the no-allocation scratch limit";
     default: return "unknown status";
   }
 }
