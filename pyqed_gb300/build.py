@@ -22,6 +22,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIBNAME = "liblindblad_gb300.so"
 LIBPATH = os.path.join(LIBDIR, LIBNAME)
+CUDA_LIB = "/usr/local/cuda/lib64"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
@@ -78,7 +79,8 @@ def build(verbose=False, force=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIBPATH + ".tmp"
-    cmd = [nvcc, "-shared"] + ARCH + ["-cudart", "static", "-o", tmp] + objs
+    cmd = ([nvcc, "-shared"] + ARCH + ["-cudart", "static", "-o", tmp] + objs +
+           ["-L" + CUDA_LIB, "-lcublas", "-Xlinker", "-rpath=" + CUDA_LIB])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

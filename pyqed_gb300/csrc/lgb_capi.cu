@@ -5,6 +5,8 @@
 #include <new>
 #include <numeric>
 
+#include <cublas_v2.h>
+
 #include "lgb_internal.h"
 
 using lgb::CtaParams;
@@ -37,6 +39,8 @@ int upload(lgb_plan* pl, T** dptr, const std::vector<T>& v) {
 }
 
 void free_plan(lgb_plan* pl) {
+  if (pl->blas) cublasDestroy(pl->blas);
+  pl->blas = nullptr;
   for (void* p : pl->allocations) cudaFree(p);
   pl->allocations.clear();
   for (int k = 0; k < 2; ++k) {
@@ -186,7 +190,7 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
     delete pl;
     return LGB_ERR_UNSUPPORTED;
   }
-  if (sched == LGB_SCHED_GEMM) {
+  if (sched == LGB_SCHED_GEMM && (prec == LGB_PREC_TF32X3 || prec == LGB_PREC_BF16X3)) {
     delete pl;
     return LGB_ERR_UNSUPPORTED;
   }
@@ -203,6 +207,12 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   std::stable_sort(pl->order.begin(), pl->order.end(), by_size);
   std::stable_sort(pl->order_w.begin(), pl->order_w.end(), by_size);
   std::stable_sort(pl->tc_order.begin(), pl->tc_order.end(), by_size);
+  if (sched == LGB_SCHED_GEMM) {
+    // every instance goes through the GEMM schedule, in order
+    pl->order.clear();
+    pl->order_w.clear();
+    pl->tc_order.clear();
+  }
   const int n_launch = (pl->order.empty() ? 0 : 1) + (pl->order_w.empty() ? 0 : 1) +
                        (pl->tc_order.empty() ? 0 : 1);
   bool ok = cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) == cudaSuccess;
@@ -241,6 +251,48 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   s = s ? s : dalloc(pl, &pl->d_y, dense ? (size_t)K * W * esz : 0);
   s = s ? s : dalloc(pl, &pl->d_err, n * sizeof(int));
   if (s == LGB_OK && pl->d_err) s = cuda_status(cudaMemset(pl->d_err, 0, n * sizeof(int)));
+  if (s == LGB_OK && sched == LGB_SCHED_GEMM) {
+    // per-instance operand slabs of the GEMM schedule (working precision)
+    const int E = pr.n_eops, D = pr.n_drive;
+    const int Kd = dense ? K : 0;
+    int maxn = 0;
+    for (int b = 0; b < n; ++b) maxn = std::max(maxn, pl->dims[b]);
+    double2* partial = nullptr;
+    int* counter = nullptr;
+    s = s ? s : dalloc(pl, &partial, (size_t)std::max(E, 1) * lgb::gemm_partial_slots(maxn) * sizeof(double2));
+    s = s ? s : dalloc(pl, &counter, sizeof(int));
+    if (s == LGB_OK) s = cuda_status(cudaMemset(counter, 0, sizeof(int)));
+    s = s ? s : dalloc(pl, &pl->d_gtmp, dense ? (size_t)maxn * maxn * sizeof(double2) : 0);
+    pl->gemm.resize(n);
+    for (int b = 0; b < n && s == LGB_OK; ++b) {
+      lgb::GemmInstance& g = pl->gemm[b];
+      const size_t NN = (size_t)pl->dims[b] * pl->dims[b];
+      g.N = pl->dims[b];
+      g.W = (Kd + 2) * g.N;
+      s = s ? s : dalloc(pl, &g.Lbuf, NN * (Kd + 2) * esz);
+      s = s ? s : dalloc(pl, &g.Rbuf, NN * (Kd + 2) * esz);
+      s = s ? s : dalloc(pl, &g.Rout, NN * esz);
+      s = s ? s : dalloc(pl, &g.Lstk, NN * Kd * esz);
+      s = s ? s : dalloc(pl, &g.Dm, pr.cops_kind == LGB_COPS_DIAG ? NN * esz : 0);
+      s = s ? s : dalloc(pl, &g.A0, D > 0 ? NN * esz : 0);
+      s = s ? s : dalloc(pl, &g.Gd, NN * D * esz);
+      s = s ? s : dalloc(pl, &g.rho, NN * esz);
+      s = s ? s : dalloc(pl, &g.racc, NN * esz);
+      s = s ? s : dalloc(pl, &g.Ot, NN * E * sizeof(double2));
+      g.partial = partial;
+      g.counter = counter;
+      g.err = pl->d_err + b;
+    }
+    if (s == LGB_OK) {
+      if (cublasCreate(&pl->blas) != CUBLAS_STATUS_SUCCESS) {
+        pl->blas = nullptr;
+        s = LGB_ERR_CUDA;
+      } else {
+        // plain library GEMMs: no reduced-precision tensor-op substitutions
+        cublasSetMathMode(pl->blas, CUBLAS_PEDANTIC_MATH);
+      }
+    }
+  }
   if (s != LGB_OK) {
     free_plan(pl);
     delete pl;
@@ -288,9 +340,35 @@ int lgb_plan_set_operators(lgb_plan_t plan, const double* H, const double* cops,
   sp.Ot = plan->d_Ot;
   sp.OtF = plan->d_OtF;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  int s = cuda_status(lgb::launch_setup(sp, pr.precision == LGB_PREC_FP64 ? 0 : 1, st));
-  if (s == LGB_OK) plan->ops_set = true;
   plan->last_stream = st;
+  int s = LGB_OK;
+  if (plan->schedule == LGB_SCHED_GEMM) {
+    s = cuda_status(lgb::launch_trace_shift(sp, st));
+    const int K = pr.n_cops;
+    for (int b = 0; b < pr.n_inst && s == LGB_OK; ++b) {
+      const long long o = plan->off[b];
+      lgb::GemmSetupArgs a;
+      a.g = plan->gemm[b];
+      a.blas = plan->blas;
+      a.fp64 = pr.precision == LGB_PREC_FP64;
+      a.H = sp.H + o;
+      a.cops = pr.cops_kind == LGB_COPS_DENSE ? sp.cops + K * o
+               : pr.cops_kind == LGB_COPS_DIAG ? sp.cops + K * plan->doff[b] : nullptr;
+      a.eops = pr.n_eops ? sp.eops + (long long)pr.n_eops * o : nullptr;
+      a.dops = pr.n_drive ? sp.dops + (long long)pr.n_drive * o : nullptr;
+      a.cops_kind = pr.cops_kind;
+      a.K = K;
+      a.E = pr.n_eops;
+      a.D = pr.n_drive;
+      a.shift = plan->d_shift + b;
+      a.doff = 0;
+      a.Gtmp = plan->d_gtmp;
+      s = lgb::gemm_setup(a, st);
+    }
+  } else {
+    s = cuda_status(lgb::launch_setup(sp, pr.precision == LGB_PREC_FP64 ? 0 : 1, st));
+  }
+  if (s == LGB_OK) plan->ops_set = true;
   return s;
 }
 
@@ -334,6 +412,32 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
   p.state_ws = plan->d_state;
   p.y_ws = plan->d_y;
   p.err = plan->d_err;
+  if (plan->schedule == LGB_SCHED_GEMM) {
+    cudaMemsetAsync(plan->d_err, 0, pr.n_inst * sizeof(int), st);
+    const long long nrows = (long long)pr.nt + pr.obs_t0;
+    for (int b = 0; b < pr.n_inst; ++b) {
+      lgb::GemmRunArgs a;
+      a.g = plan->gemm[b];
+      a.blas = plan->blas;
+      a.fp64 = pr.precision == LGB_PREC_FP64;
+      a.Kdense = pr.cops_kind == LGB_COPS_DENSE ? pr.n_cops : 0;
+      a.D = pr.n_drive;
+      a.E = pr.n_eops;
+      a.nt = pr.nt;
+      a.obs_t0 = pr.obs_t0;
+      a.store_every = pr.store_every;
+      a.diag = pr.cops_kind == LGB_COPS_DIAG && pr.n_cops > 0;
+      a.dt = pr.dt;
+      a.rho0 = p.rho0 + plan->off[b];
+      a.drive = pr.n_drive ? drive_samples + (pr.drive_shared ? 0 : (long long)b * pr.n_drive * pr.nt) : nullptr;
+      a.obs_out = p.obs_out ? p.obs_out + (long long)b * nrows * pr.n_eops : nullptr;
+      a.rho_out = p.rho_out ? p.rho_out + plan->off[b] : nullptr;
+      a.states_out = p.states_out ? p.states_out + plan->soff[b] : nullptr;
+      const int r = lgb::gemm_propagate(a, st);
+      if (r != LGB_OK) return r;
+    }
+    return LGB_OK;
+  }
   // Up to three kernels (wide FP32 CTA, FP32 CTA, tensor-core) cover the
   // batch; the first runs on the caller's stream, the others on forked
   // streams joined back before return.
@@ -391,6 +495,14 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
   info->smem_bytes = std::max(std::max(plan->smem_bytes, plan->smem_w), plan->tc_smem);
   info->launches_per_propagate = (plan->order.empty() ? 0 : 1) + (plan->order_w.empty() ? 0 : 1) +
                                  (plan->tc_order.empty() ? 0 : 1);
+  if (plan->schedule == LGB_SCHED_GEMM) {
+    // per instance: init (+ t0 observables) + per step (drive) + 4 x (G1, G2, epilogue)
+    const lgb_problem_t& pr = plan->prob;
+    const int per_stage = (pr.cops_kind == LGB_COPS_DENSE ? 2 : 1) + 1;
+    info->launches_per_propagate =
+        pr.n_inst * (1 + (pr.obs_t0 && pr.n_eops ? 1 : 0) +
+                     pr.nt * (4 * per_stage + (pr.n_drive > 0 ? 1 : 0)));
+  }
   info->workspace_bytes = (int64_t)plan->ws_bytes;
   info->flops_per_step = plan->flops_per_step;
   return LGB_OK;

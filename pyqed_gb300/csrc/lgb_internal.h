@@ -7,6 +7,8 @@
 #include <vector>
 
 #include "../../include/lindblad_gb300.h"
+
+struct cublasContext;
 #include "lgb_common.cuh"
 
 namespace lgb {
@@ -45,6 +47,53 @@ struct SetupParams {
   float2* OtF;  // FP32 copy of Ot (FP32-working plans only)
 };
 cudaError_t launch_setup(const SetupParams& p, int precision, cudaStream_t stream);
+cudaError_t launch_trace_shift(const SetupParams& p, cudaStream_t stream);
+
+// ---- grid-wide GEMM schedule (lgb_gemm.cu) ----------------------------------------
+struct GemmInstance {
+  int N = 0, W = 0;              // dimension; W = (K_dense + 2) N, the GEMM K extent
+  void* Lbuf = nullptr;          // N x W   [A | X | T_1 .. T_K]      (working precision)
+  void* Rbuf = nullptr;          // W x N   [X ; A^dag ; L_k^dag]
+  void* Rout = nullptr;          // N x N   RHS
+  void* Lstk = nullptr;          // K x N x N collapse operators
+  void* Dm = nullptr;            // N x N   diagonal-collapse dissipator matrix
+  void* A0 = nullptr;            // N x N   static A of a driven instance
+  void* Gd = nullptr;            // D x N x N drive terms i H_d
+  void* rho = nullptr;           // N x N
+  void* racc = nullptr;          // N x N   RK4 sum
+  double2* Ot = nullptr;         // E x N x N observables transposed (FP64)
+  double2* partial = nullptr;    // E x grid observable partials
+  int* counter = nullptr;        // last-block ticket
+  int* err = nullptr;            // instance status
+};
+struct GemmSetupArgs {
+  GemmInstance g;
+  cublasContext* blas = nullptr;
+  bool fp64 = false;
+  const double2* H = nullptr;
+  const double2* cops = nullptr;  // this instance's collapse operators
+  const double2* eops = nullptr;
+  const double2* dops = nullptr;
+  int cops_kind = 0, K = 0, E = 0, D = 0;
+  const double* shift = nullptr;  // device, Re Tr(H)/N
+  long long doff = 0;             // packed-diagonal base of this instance (diag kind)
+  double2* Gtmp = nullptr;        // N x N FP64 scratch for sum_k L_k^dag L_k
+};
+struct GemmRunArgs {
+  GemmInstance g;
+  cublasContext* blas = nullptr;
+  bool fp64 = false;
+  int Kdense = 0, D = 0, E = 0, nt = 0, obs_t0 = 0, store_every = 0, diag = 0;
+  double dt = 0.0;
+  const double2* rho0 = nullptr;
+  const double* drive = nullptr;   // [D][nt] for this instance
+  double2* obs_out = nullptr;      // this instance's rows
+  double2* rho_out = nullptr;
+  double2* states_out = nullptr;
+};
+size_t gemm_partial_slots(int N);
+int gemm_setup(const GemmSetupArgs& a, cudaStream_t st);
+int gemm_propagate(const GemmRunArgs& a, cudaStream_t st);
 
 }  // namespace lgb
 
@@ -94,4 +143,8 @@ struct lgb_plan {
   void* d_y = nullptr;
   int* d_err = nullptr;
   std::vector<void*> allocations;
+  // grid-wide GEMM schedule
+  cublasContext* blas = nullptr;
+  std::vector<lgb::GemmInstance> gemm;
+  double2* d_gtmp = nullptr;
 };

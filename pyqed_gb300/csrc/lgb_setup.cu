@@ -120,6 +120,11 @@ __global__ void setup_kernel(SetupParams p) {
 
 }  // namespace
 
+cudaError_t launch_trace_shift(const SetupParams& p, cudaStream_t stream) {
+  trace_shift_kernel<<<p.n_inst, 256, 0, stream>>>(p);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_setup(const SetupParams& p, int precision, cudaStream_t stream) {
   trace_shift_kernel<<<p.n_inst, 256, 0, stream>>>(p);
   cudaError_t e = cudaGetLastError();

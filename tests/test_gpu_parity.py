@@ -252,3 +252,78 @@ def test_split_solver_run_matches_fp64():
     r64 = sol.run(jc["rho0"], dt=jc["dt"], Nt=200, e_ops=jc["e_ops"], precision="fp64")
     r32 = sol.run(jc["rho0"], dt=jc["dt"], Nt=200, e_ops=jc["e_ops"], precision="3xtf32")
     assert np.abs(r32.observables - r64.observables).max() < TOL32
+
+
+# ---- grid-wide GEMM schedule (large N) ----------------------------------------------
+
+def _digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype=np.complex128).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_gue256_golden(golden, prec, tol):
+    g = golden("gue256")
+    w = W.gue_instance(N=256, K=4, seed=2)
+    if _digest(w["H"], *w["c_ops"], w["rho0"]) != str(g["digest"]):
+        pytest.skip("numpy's generator stream differs from the fixture's")
+    sol = LindbladSolver(w["H"], w["c_ops"])
+    rho = sol.evolve_fast(w["rho0"].copy(), dt=float(g["dt"]), Nt=int(g["nt"]), precision=prec)
+    assert np.abs(rho - g["rho"]).max() < tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_gue1024_golden(golden, prec, tol):
+    g = golden("gue1024")
+    w = W.gue_instance(N=1024, K=8, scale=0.02, rank=4, seed=4, dt=0.005, nt=1000)
+    if _digest(w["H"], *w["c_ops"], w["rho0"]) != str(g["digest"]):
+        pytest.skip("numpy's generator stream differs from the fixture's")
+    sol = LindbladSolver(w["H"], w["c_ops"])
+    rho = sol.evolve_fast(w["rho0"].copy(), dt=float(g["dt"]), Nt=int(g["nt"]), precision=prec)
+    assert np.abs(rho[:8, :] - g["rows"]).max() < tol
+    assert np.abs(np.diag(rho) - g["diag"]).max() < tol
+    assert abs(np.trace(rho) - g["trace"]) < tol * 10
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+@pytest.mark.parametrize("kind", ["dense", "diag"])
+def test_gemm_schedule_vs_oracle(prec, tol, kind):
+    rng = np.random.default_rng(31)
+    dims = [3, 20, 33]
+    H, cops, rho0, eops = [], [], [], []
+    for N in dims:
+        h, c, r, o = _random_instance(rng, N, 3)
+        if kind == "diag":
+            c = [np.diag((rng.standard_normal(N) + 1j * rng.standard_normal(N)) * 0.1) for _ in range(3)]
+        H.append(h), cops.append(c), rho0.append(r), eops.append([o, h])
+    res = propagate_batch(H, cops, rho0, 0.03, 9, e_ops=eops, obs_t0=True, store_every=3,
+                          precision=prec, schedule="gemm")
+    assert res["info"]["schedule"] == "gemm"
+    for b, N in enumerate(dims):
+        obs, states = O.lindblad(H[b], rho0[b], cops[b], eops[b], Nt=9, dt=0.03)
+        assert np.abs(res["rho"][b] - states[-1]).max() < tol
+        assert np.abs(res["observables"][b] - obs).max() < tol * N
+        for k in range(3):
+            assert np.abs(res["states"][b][k] - states[3 * k + 2]).max() < tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+def test_gemm_schedule_driven_vs_oracle(prec, tol):
+    rng = np.random.default_rng(32)
+    dims = [12, 100]
+    E = W.gp_pulse(8, 0.02, seed=3, amp=0.4)
+    H0 = [W.gue_matrix(rng, N) for N in dims]
+    mu = [W.gue_matrix(rng, N) for N in dims]
+    cops = [[(rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) * 0.02 for _ in range(2)]
+            for N in dims]
+    rho0 = [np.eye(N, dtype=complex) / N for N in dims]
+    res = propagate_batch(H0, cops, rho0, 0.02, 8, e_ops=[[m] for m in mu], obs_t0=False,
+                          precision=prec, drive_ops=[[m] for m in mu], drive=E[None, :])
+    assert res["info"]["schedule"] == "gemm"  # N = 100 exceeds the CTA kernels
+    for b in range(2):
+        obs, states = O.lindblad_driven([H0[b], [mu[b], E]], rho0[b], cops[b], [mu[b]], Nt=8, dt=0.02)
+        assert np.abs(res["rho"][b] - states[-1]).max() < tol
+        assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < tol * 10
