@@ -78,9 +78,11 @@ def main():
     g = W.gue_instance(N=1024, K=8, scale=0.02, rank=4, seed=4, dt=0.005, nt=1000)
     nt = 2
     rho = oqs._fast_lindblad(g["H"], g["rho0"].copy(), g["c_ops"], e_ops=[], Nt=nt, dt=g["dt"])
-    out["gue1024"] = dict(digest=digest(g["H"], *g["c_ops"], g["rho0"]), dt=g["dt"], nt=nt,
-                          rows=rho[:8, :], diag=np.diag(rho).copy(), trace=np.trace(rho),
-                          fro=np.linalg.norm(rho))
+    # rho0 comes from a QR factorisation whose last bits depend on the BLAS
+    # build, so the operators are pinned by digest and rho0 by its diagonal
+    out["gue1024"] = dict(digest_ops=digest(g["H"], *g["c_ops"]), rho0_diag=np.diag(g["rho0"]).copy(),
+                          dt=g["dt"], nt=nt, rows=rho[:8, :], diag=np.diag(rho).copy(),
+                          trace=np.trace(rho), fro=np.linalg.norm(rho))
 
     # 5. exciton correlation functions, 8 instances spanning n = 8..64
     dims = W.exciton_dims()
