@@ -83,9 +83,16 @@ typedef struct {
   int32_t precision;    /* LGB_PREC_*                                              */
   int32_t schedule;     /* LGB_SCHED_*                                             */
   int32_t drive_shared; /* 1: one sample set f_i(t_k) for all instances           */
-  int32_t flags;        /* reserved, must be 0                                     */
+  int32_t flags;        /* LGB_FLAG_* (0 or LGB_FLAG_ADJOINT)                      */
   double dt;            /* time step                                               */
+  int32_t checkpoint_every; /* adjoint plans: keep rho every C steps (0: ~sqrt(nt)) */
+  int32_t reserved;     /* must be 0                                               */
 } lgb_problem_t;
+
+/* Plan flags. */
+enum {
+  LGB_FLAG_ADJOINT = 1  /* keep checkpoints during propagate for lgb_plan_adjoint */
+};
 
 /* Library version: major*10000 + minor*100 + patch. */
 int lgb_get_version(void);
@@ -132,6 +139,27 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
  * LGB_ERR_TIMEOUT) of the last propagate into flags_host[n_inst];
  * synchronises the plan's last stream.  Returns the first non-OK flag. */
 int lgb_plan_errors(lgb_plan_t plan, int32_t* flags_host);
+
+/* Discrete adjoint of the last lgb_plan_propagate (plans created with
+ * LGB_FLAG_ADJOINT: FP32, N <= 64, dense or no collapse operators, no stored
+ * states).  Propagates the costate backwards with the adjoint generator,
+ * recomputing the stage inputs segment by segment from the checkpoints kept
+ * by propagate.  No counterpart in the reference, which has no gradients;
+ * the forward map it differentiates is _lindblad_driven
+ * (pyqed/oqs.py:1699-1806) with rk4 (pyqed/phys.py:1051-1064).
+ *   rho0        the initial states given to propagate (device, packed c128)
+ *   drive       the drive samples given to propagate
+ *   obs_grad    [n_inst][nt + obs_t0][n_eops] complex128: dJ/dRe(o) + i dJ/dIm(o)
+ *               for every observable o = Tr[O rho]
+ *   dE_out      [n_inst][n_drive][nt] doubles: dJ/df_d(t_{k+1}) per instance, or NULL
+ *   dscale_out  [n_inst][n_cops] doubles: dJ/ds_j for L_j -> sqrt(s_j) L_j at s_j = 1
+ *               (divide by gamma_j for dJ/dgamma_j when L_j = sqrt(gamma_j) L^_j), or NULL
+ *   dH_out      packed complex128 Gamma per instance, dJ = Re Tr[Gamma^dag dH0], or NULL
+ *   drho0_out   packed complex128 dJ/drho0 in the same convention, or NULL
+ * Asynchronous on `stream`. */
+int lgb_plan_adjoint(lgb_plan_t plan, const double* rho0, const double* drive,
+                     const double* obs_grad, double* dE_out, double* dscale_out, double* dH_out,
+                     double* drho0_out, void* stream);
 
 /* Plan introspection: the schedule and precision in use, the bytes of
  * device workspace, the dynamic shared memory per CTA and the number of

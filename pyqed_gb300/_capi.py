@@ -39,8 +39,9 @@ SCHED_NAME = {v: k for k, v in SCHED.items()}
 EXPORTS = [
     "lgb_get_version", "lgb_status_string", "lgb_plan_create", "lgb_plan_destroy",
     "lgb_plan_set_operators", "lgb_plan_propagate", "lgb_plan_errors", "lgb_plan_get_info",
-    "lgb_propagate_noalloc",
+    "lgb_propagate_noalloc", "lgb_plan_adjoint",
 ]
+FLAG_ADJOINT = 1
 
 
 class LindbladError(RuntimeError):
@@ -57,6 +58,7 @@ class Problem(ctypes.Structure):
         ("obs_t0", ctypes.c_int32), ("store_every", ctypes.c_int32),
         ("precision", ctypes.c_int32), ("schedule", ctypes.c_int32),
         ("drive_shared", ctypes.c_int32), ("flags", ctypes.c_int32), ("dt", ctypes.c_double),
+        ("checkpoint_every", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
 
 
@@ -107,6 +109,8 @@ def lib():
     L.lgb_plan_errors.argtypes = [vp, ctypes.POINTER(i32)]
     L.lgb_plan_get_info.restype = ctypes.c_int
     L.lgb_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+    L.lgb_plan_adjoint.restype = ctypes.c_int
+    L.lgb_plan_adjoint.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, vp]
     L.lgb_propagate_noalloc.restype = ctypes.c_int
     L.lgb_propagate_noalloc.argtypes = [dp, i32, dp, i32, i32, dp, i32, dp, i32, ctypes.c_double,
                                         i32, dp, dp, dp, vp]

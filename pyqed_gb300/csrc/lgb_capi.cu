@@ -1,6 +1,7 @@
 // C-ABI entry points (include/lindblad_gb300.h): plan set-up, operator
 // upload, propagation and error reporting.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <numeric>
@@ -56,8 +57,17 @@ void free_plan(lgb_plan* pl) {
 int validate(const lgb_problem_t* pr, const int32_t* dims) {
   if (pr == nullptr || dims == nullptr) return LGB_ERR_INVALID_ARG;
   if (pr->n_inst < 1 || pr->n_cops < 0 || pr->n_eops < 0 || pr->n_eops > 16 || pr->n_drive < 0 ||
-      pr->n_drive > 4 || pr->nt < 0 || pr->store_every < 0 || pr->flags != 0)
+      pr->n_drive > 4 || pr->nt < 0 || pr->store_every < 0 ||
+      (pr->flags & ~LGB_FLAG_ADJOINT) != 0 || pr->checkpoint_every < 0 || pr->reserved != 0)
     return LGB_ERR_INVALID_ARG;
+  if (pr->flags & LGB_FLAG_ADJOINT) {
+    // the adjoint runs on the FP32 CTA kernel with dense (or no) collapse operators
+    if (pr->precision != LGB_PREC_FP32 || pr->cops_kind == LGB_COPS_DIAG || pr->store_every != 0 ||
+        pr->schedule == LGB_SCHED_GEMM || pr->n_cops > 4)
+      return LGB_ERR_UNSUPPORTED;
+    for (int b = 0; b < pr->n_inst; ++b)
+      if (dims[b] > 64) return LGB_ERR_UNSUPPORTED;
+  }
   if (pr->cops_kind < LGB_COPS_NONE || pr->cops_kind > LGB_COPS_DIAG) return LGB_ERR_INVALID_ARG;
   if (pr->cops_kind == LGB_COPS_NONE && pr->n_cops != 0) return LGB_ERR_INVALID_ARG;
   if (pr->cops_kind != LGB_COPS_NONE && pr->n_cops == 0) return LGB_ERR_INVALID_ARG;
@@ -117,7 +127,15 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   pl->woff.resize(n);
   pl->soff.resize(n);
   pl->place.assign(n, 0);
-  pl->n_store = pr.store_every > 0 ? pr.nt / pr.store_every : 0;
+  pl->adjoint = (pr.flags & LGB_FLAG_ADJOINT) != 0;
+  if (pl->adjoint) {
+    int c = pr.checkpoint_every;
+    if (c <= 0) c = std::max(1, (int)std::lround(std::sqrt((double)std::max(pr.nt, 1))));
+    pl->ckpt_every = c;
+    pl->n_store = pr.nt / c;  // checkpoints rho_C, rho_2C, ...
+  } else {
+    pl->n_store = pr.store_every > 0 ? pr.nt / pr.store_every : 0;
+  }
   const int K = pr.n_cops;
   const bool dense = pr.cops_kind == LGB_COPS_DENSE;
   const bool split = prec == LGB_PREC_TF32X3 || prec == LGB_PREC_BF16X3;
@@ -135,7 +153,8 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
     pl->off[b] = pl->tot_off;
     pl->doff[b] = pl->tot_doff;
     pl->woff[b] = pl->tot_woff;
-    pl->soff[b] = pl->n_store * pl->tot_off;
+    // user states: per instance contiguous; adjoint checkpoints: [n_ckpt][packed]
+    pl->soff[b] = pl->adjoint ? pl->tot_off : pl->n_store * pl->tot_off;
     pl->tot_off += N * N;
     pl->tot_doff += N;
     pl->tot_woff += (long long)NP * (NP + pl->padc);
@@ -251,6 +270,19 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   s = s ? s : dalloc(pl, &pl->d_y, dense ? (size_t)K * W * esz : 0);
   s = s ? s : dalloc(pl, &pl->d_err, n * sizeof(int));
   if (s == LGB_OK && pl->d_err) s = cuda_status(cudaMemset(pl->d_err, 0, n * sizeof(int)));
+  if (s == LGB_OK && pl->adjoint) {
+    const long long W = pl->tot_woff;
+    const int C = pl->ckpt_every;
+    s = s ? s : dalloc(pl, &pl->d_ckpt, (size_t)std::max<long long>(pl->n_store, 1) * pl->tot_off * sizeof(double2));
+    s = s ? s : dalloc(pl, &pl->d_ybuf, (size_t)4 * C * W * sizeof(float2));
+    s = s ? s : dalloc(pl, &pl->d_lam, (size_t)W * sizeof(float2));
+    s = s ? s : dalloc(pl, &pl->d_lc, (size_t)std::max(K, 1) * W * sizeof(float2));
+    s = s ? s : dalloc(pl, &pl->d_gkt, (size_t)std::max(K, 1) * W * sizeof(float2));
+    s = s ? s : dalloc(pl, &pl->d_macc, (size_t)W * sizeof(float2));
+    int maxnp = 0;
+    for (int b = 0; b < n; ++b) maxnp = std::max(maxnp, pl->npad[b]);
+    pl->adj_smem = lgb::adjoint_smem_bytes(maxnp, K);
+  }
   if (s == LGB_OK && sched == LGB_SCHED_GEMM) {
     // per-instance operand slabs of the GEMM schedule (working precision)
     const int E = pr.n_eops, D = pr.n_drive;
@@ -412,6 +444,13 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
   p.state_ws = plan->d_state;
   p.y_ws = plan->d_y;
   p.err = plan->d_err;
+  if (plan->adjoint) {
+    // checkpoints for lgb_plan_adjoint: rho_C, rho_2C, ... for the whole batch
+    if (states_out != nullptr) return LGB_ERR_INVALID_ARG;
+    p.store_every = plan->ckpt_every;
+    p.states_out = plan->d_ckpt;
+    p.state_stride = plan->tot_off;
+  }
   if (plan->schedule == LGB_SCHED_GEMM) {
     cudaMemsetAsync(plan->d_err, 0, pr.n_inst * sizeof(int), st);
     const long long nrows = (long long)pr.nt + pr.obs_t0;
@@ -474,6 +513,105 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
     if (e == cudaSuccess && k > 0) e = cudaEventRecord(plan->ev_join[k - 1], s_k);
   }
   for (int k = 1; k < nl && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, plan->ev_join[k - 1], 0);
+  return cuda_status(e);
+}
+
+int lgb_plan_adjoint(lgb_plan_t plan, const double* rho0, const double* drive,
+                     const double* obs_grad, double* dE_out, double* dscale_out, double* dH_out,
+                     double* drho0_out, void* stream) {
+  if (plan == nullptr || rho0 == nullptr) return LGB_ERR_INVALID_ARG;
+  if (!plan->adjoint) return LGB_ERR_STATE;
+  if (!plan->ops_set) return LGB_ERR_STATE;
+  const lgb_problem_t& pr = plan->prob;
+  if (pr.n_drive > 0 && pr.nt > 0 && drive == nullptr) return LGB_ERR_INVALID_ARG;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  plan->last_stream = st;
+  const int n = pr.n_inst;
+  const int K = pr.cops_kind == LGB_COPS_DENSE ? pr.n_cops : 0;
+  const int C = plan->ckpt_every;
+  const int nseg = (pr.nt + C - 1) / C;
+  cudaError_t e = cudaSuccess;
+  if (dscale_out != nullptr && K > 0) e = cudaMemsetAsync(dscale_out, 0, (size_t)n * K * sizeof(double), st);
+  if (dE_out != nullptr && pr.n_drive > 0 && e == cudaSuccess)
+    e = cudaMemsetAsync(dE_out, 0, (size_t)n * pr.n_drive * pr.nt * sizeof(double), st);
+  if (e != cudaSuccess) return LGB_ERR_CUDA;
+
+  CtaParams f{};  // recompute pass: the forward kernel recording stage inputs
+  f.n_inst = n;
+  f.n_cops = pr.n_cops;
+  f.cops_kind = pr.cops_kind;
+  f.n_eops = 0;
+  f.n_drive = pr.n_drive;
+  f.obs_t0 = 0;
+  f.store_every = 0;
+  f.drive_shared = pr.drive_shared;
+  f.dt = pr.dt;
+  f.order = plan->d_order;
+  f.dims = plan->d_dims;
+  f.npad = plan->d_npad;
+  f.off = plan->d_off;
+  f.woff = plan->d_woff;
+  f.soff = plan->d_soff;
+  f.place = plan->d_place;
+  f.At = plan->d_At;
+  f.Lt = plan->d_Lt;
+  f.Dm = plan->d_Dm;
+  f.Gt = plan->d_Gt;
+  f.Ot = plan->d_Ot;
+  f.OtF = plan->d_OtF;
+  f.state_ws = plan->d_state;
+  f.y_ws = plan->d_y;
+  f.err = plan->d_err;
+  f.smem_bytes = plan->smem_bytes;
+  f.drive_ld = pr.nt;
+  f.ystore = plan->d_ybuf;
+  f.ycap = C;
+
+  lgb::AdjParams a{};
+  a.n_inst = n;
+  a.n_cops = K;
+  a.n_drive = pr.n_drive;
+  a.n_eops = pr.n_eops;
+  a.nt = pr.nt;
+  a.ycap = C;
+  a.drive_ld = pr.nt;
+  a.drive_shared = pr.drive_shared;
+  a.obs_t0 = pr.obs_t0;
+  a.smem_bytes = plan->adj_smem;
+  a.dt = pr.dt;
+  a.order = plan->d_order;
+  a.dims = plan->d_dims;
+  a.npad = plan->d_npad;
+  a.woff = plan->d_woff;
+  a.At = reinterpret_cast<const float2*>(plan->d_At);
+  a.Gt = reinterpret_cast<const float2*>(plan->d_Gt);
+  a.Lt = reinterpret_cast<const float2*>(plan->d_Lt);
+  a.Lc = plan->d_lc;
+  a.GkT = plan->d_gkt;
+  a.Macc = plan->d_macc;
+  a.lam = plan->d_lam;
+  a.ys = reinterpret_cast<const float2*>(plan->d_ybuf);
+  a.Ot = plan->d_Ot;
+  a.drive = drive;
+  a.obs_grad = reinterpret_cast<const double2*>(obs_grad);
+  a.dE = dE_out;
+  a.dscale = dscale_out;
+  for (int sg = nseg - 1; sg >= 0 && e == cudaSuccess; --sg) {
+    const int seg0 = sg * C;
+    const int len = std::min(C, pr.nt - seg0);
+    f.nt = len;
+    f.rho0 = sg == 0 ? reinterpret_cast<const double2*>(rho0)
+                     : plan->d_ckpt + (long long)(sg - 1) * plan->tot_off;
+    f.drive = drive != nullptr ? drive + seg0 : nullptr;
+    e = lgb::launch_cta_rk4(f, 1, n, st, false);
+    a.seg0 = seg0;
+    a.seg_len = len;
+    a.first_segment = sg == nseg - 1;
+    if (e == cudaSuccess) e = lgb::launch_adjoint_segment(a, n, st);
+  }
+  if (e == cudaSuccess && (drho0_out != nullptr || dH_out != nullptr))
+    e = lgb::launch_adjoint_finish(a, plan->d_off, reinterpret_cast<double2*>(drho0_out),
+                                   reinterpret_cast<double2*>(dH_out), st);
   return cuda_status(e);
 }
 

@@ -82,6 +82,10 @@ struct CtaParams {
   void* y_ws;                // Y_k^T scratch, n_cops x NP x NPS per instance (when not in smem)
   int* err;                  // per-instance status
   int smem_bytes;            // dynamic shared memory of the launch
+  int drive_ld;              // samples per drive term and instance (0: nt)
+  long long state_stride;    // complex elements between stored states (0: N*N)
+  void* ystore;              // optional: every stage input, 4 * ycap x NP x NPS per instance
+  int ycap;                  // steps held per instance in ystore
 };
 
 }  // namespace lgb

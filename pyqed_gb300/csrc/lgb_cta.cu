@@ -52,7 +52,7 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-template <typename T, int NT, int ROUNDS, bool SREG>
+template <typename T, int NT, int ROUNDS, bool SREG, bool YS = false>
 __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsigned char* smem,
                                          double2 (*sRed)[kMaxEops], int* sFlag) {
   constexpr int kWarps = NT / 32;
@@ -212,19 +212,42 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
     return anybad;
   };
 
+  // optional record of every stage input (the recompute pass of the adjoint)
+  T2* ys = (YS && p.ystore != nullptr)
+               ? reinterpret_cast<T2*>(p.ystore) + 4LL * p.ycap * wo : nullptr;
+  auto ystore = [&](int slot, int i, int j, T2 v) {
+    if constexpr (YS) {
+      if (ys != nullptr) ys[(long long)slot * MS + i * NPS + j] = v;
+    }
+  };
+  if (YS && ys != nullptr) {
+#pragma unroll
+    for (int r = 0; r < ROUNDS; ++r) {
+      if (!act[r]) continue;
+#pragma unroll
+      for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int i = 4 * ty[r] + ii, j = tx[r] + nT * jj;
+          ystore(0, i, j, sX[i * NPS + j]);
+        }
+    }
+  }
+
   if (tid == 0) p.err[b] = 0;
   __syncthreads();
   if (p.obs_t0) reduce_state(0);
 
+  const int dld = p.drive_ld > 0 ? p.drive_ld : p.nt;
   const double* drv = p.drive;
-  if (p.n_drive > 0 && !p.drive_shared) drv += (long long)b * p.n_drive * p.nt;
+  if (p.n_drive > 0 && !p.drive_shared) drv += (long long)b * p.n_drive * dld;
 
   for (int step = 0; step < p.nt; ++step) {
     if (p.n_drive > 0) {
       // H(t_{k+1}) = H0 - sum_d f_d(t_{k+1}) H_d  ->  A = A0 + sum_d f_d (i H_d)
       T f[4];
 #pragma unroll
-      for (int d = 0; d < 4; ++d) f[d] = (d < p.n_drive) ? (T)drv[(long long)d * p.nt + step] : (T)0;
+      for (int d = 0; d < 4; ++d) f[d] = (d < p.n_drive) ? (T)drv[(long long)d * dld + step] : (T)0;
       for (int i = tid; i < MS; i += NT) {
         T2 a = At0[i];
 #pragma unroll
@@ -369,6 +392,11 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
             }
             sX[i * NPS + j] = xn;
             sXt[j * NPS + i] = xn;
+            if (stage < 3) {
+              ystore(step * 4 + stage + 1, i, j, xn);
+            } else if (step + 1 < p.nt) {
+              ystore((step + 1) * 4, i, j, xn);
+            }
           }
         }
       }
@@ -383,7 +411,8 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
     }
     if (p.store_every > 0 && p.states_out != nullptr && ((step + 1) % p.store_every) == 0) {
       const long long si = (step + 1) / p.store_every - 1;
-      double2* dst = p.states_out + p.soff[b] + si * (long long)N * N;
+      double2* dst = p.states_out + p.soff[b] +
+                     si * (p.state_stride > 0 ? p.state_stride : (long long)N * N);
 #pragma unroll
       for (int r = 0; r < ROUNDS; ++r) {
         if (!act[r]) continue;
@@ -452,6 +481,15 @@ __global__ void __launch_bounds__(kThreads, 1) cta_rk4_kernel(CtaParams p) {
   }
 }
 
+// FP32, N <= 64, recording every stage input (the adjoint's recompute pass).
+__global__ void __launch_bounds__(kThreads, 1) cta_rk4_record_kernel(CtaParams p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double2 sRed[kThreads / 32][kMaxEops];
+  __shared__ int sFlag[kThreads / 32];
+  const int b = p.order[blockIdx.x];
+  cta_body<float, kThreads, 1, true, true>(p, b, smem, sRed, sFlag);
+}
+
 // FP32, 64 < N <= 76: one 4x4 tile per thread, state in registers.
 __global__ void __launch_bounds__(kThreadsWide, 1) cta_rk4_wide_kernel(CtaParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -472,7 +510,12 @@ cudaError_t launch_cta_rk4(const CtaParams& p, int precision, int n_blocks, cuda
                            bool wide) {
   if (n_blocks <= 0) return cudaSuccess;
   cudaError_t e;
-  if (wide) {
+  if (p.ystore != nullptr) {
+    e = cudaFuncSetAttribute(cta_rk4_record_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             p.smem_bytes);
+    if (e != cudaSuccess) return e;
+    cta_rk4_record_kernel<<<n_blocks, kThreads, p.smem_bytes, stream>>>(p);
+  } else if (wide) {
     e = cudaFuncSetAttribute(cta_rk4_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              p.smem_bytes);
     if (e != cudaSuccess) return e;

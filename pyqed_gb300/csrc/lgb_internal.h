@@ -26,6 +26,34 @@ int tc_smem_bytes(int precision, int npad);
 cudaError_t launch_tc_rk4(const CtaParams& p, int precision, const int* order, int n_items,
                           int* queue, int grid, cudaStream_t stream);
 
+// ---- discrete adjoint (lgb_adjoint.cu) ------------------------------------------
+struct AdjParams {
+  int n_inst, n_cops, n_drive, n_eops, nt, seg0, seg_len, ycap, drive_ld, drive_shared, obs_t0;
+  int first_segment, smem_bytes;
+  double dt;
+  const int* order;
+  const int* dims;
+  const int* npad;
+  const long long* woff;
+  const float2* At;      // forward A0^T (working FP32)
+  const float2* Gt;      // (i H_d)^T
+  const float2* Lt;      // L_k^T
+  float2* Lc;            // scratch: conj(L_k) row-major
+  float2* GkT;           // scratch: (L_k^dag L_k)^T
+  float2* Macc;          // sum over stages of P - Q (the H0 gradient before Gamma = i M^dag)
+  float2* lam;           // costate
+  const float2* ys;      // stage inputs of the segment
+  const double2* Ot;     // observables transposed (FP64)
+  const double* drive;   // drive samples, [inst][n_drive][drive_ld]
+  const double2* obs_grad;
+  double* dE;            // [n_inst][n_drive][nt]
+  double* dscale;        // [n_inst][n_cops], accumulated
+};
+int adjoint_smem_bytes(int npad, int K);
+cudaError_t launch_adjoint_segment(const AdjParams& p, int n_blocks, cudaStream_t st);
+cudaError_t launch_adjoint_finish(const AdjParams& p, const long long* off, double2* drho0,
+                                  double2* dH, cudaStream_t st);
+
 // ---- operator preparation (lgb_setup.cu) -------------------------------------
 struct SetupParams {
   int n_inst, n_cops, cops_kind, n_eops, n_drive, padc;
@@ -143,6 +171,16 @@ struct lgb_plan {
   void* d_y = nullptr;
   int* d_err = nullptr;
   std::vector<void*> allocations;
+  // adjoint (plans created with LGB_FLAG_ADJOINT)
+  bool adjoint = false;
+  int ckpt_every = 0;
+  double2* d_ckpt = nullptr;     // [n_ckpt][packed] checkpoints rho_C, rho_2C, ...
+  void* d_ybuf = nullptr;        // stage inputs of one segment, 4 C x NP x NPS per instance
+  float2* d_lam = nullptr;
+  float2* d_lc = nullptr;
+  float2* d_gkt = nullptr;
+  float2* d_macc = nullptr;
+  int adj_smem = 0;
   // grid-wide GEMM schedule
   cublasContext* blas = nullptr;
   std::vector<lgb::GemmInstance> gemm;

@@ -74,7 +74,7 @@ class Propagator:
 
     def __init__(self, dims, *, nt, dt, n_cops=0, cops_kind="none", n_eops=0, n_drive=0,
                  obs_t0=False, store_every=0, precision="fp32", schedule="auto",
-                 drive_shared=True, device=None):
+                 drive_shared=True, device=None, flags=0, checkpoint_every=0):
         self.device = _device(device)
         self.dims = np.asarray(dims, dtype=np.int32)
         self.n_inst = int(self.dims.size)
@@ -93,8 +93,8 @@ class Propagator:
             n_inst=self.n_inst, n_cops=self.n_cops, cops_kind=self.cops_kind,
             n_eops=self.n_eops, n_drive=self.n_drive, nt=self.nt, obs_t0=int(self.obs_t0),
             store_every=self.store_every, precision=C.PREC[precision],
-            schedule=C.SCHED[schedule], drive_shared=int(self.drive_shared), flags=0,
-            dt=self.dt)
+            schedule=C.SCHED[schedule], drive_shared=int(self.drive_shared), flags=int(flags),
+            dt=self.dt, checkpoint_every=int(checkpoint_every), reserved=0)
         self._lib = C.lib()
         self._plan = ctypes.c_void_p()
         with torch.cuda.device(self.device):
