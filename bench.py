@@ -275,11 +275,60 @@ def run_gpu(args):
                        api="pyqed_gb300.engine.Propagator.set_operators + propagate "
                            "(C ABI lgb_plan_set_operators/lgb_plan_propagate)")
     line["clocks"] = ch["clocks"]
+    if not args.no_adjoint:
+        line["adjoint"] = measure_adjoint(args, dev)
     # CPU baseline (oracle port of the reference's dense algorithm) and accuracy
     if not args.no_cpu:
         line["cpu_baseline"], line["accuracy"] = cpu_baseline_and_accuracy(
             wl, results, args, chosen)
     print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# adjoint cost: the metric's bwd/fwd on the driven workload
+# ---------------------------------------------------------------------------
+def measure_adjoint(args, dev):
+    """256 driven instances, N=64, K=2, H(t) = H0 - E(t) mu, 2000 steps,
+    loss sum_t |<O>(t) - target(t)|^2, gradients w.r.t. E(t) and gamma_k,
+    checkpoints every 45 steps.  fwd = propagate with checkpoints,
+    bwd = lgb_plan_adjoint (segment recompute + backward costate)."""
+    import torch
+    from pyqed_gb300 import workloads as W
+    from pyqed_gb300.adjoint import DrivenBatch
+    n_inst = args.adj_n_inst
+    d = W.driven_batch(n_inst=n_inst, nt=args.adj_nt)
+    nt = d["nt"]
+    batch = DrivenBatch(d["H0"], [[m] for m in d["mu"]], d["L"], d["rho0"], [[o] for o in d["O"]],
+                        d["dt"], nt, checkpoint_every=45, device=dev)
+    target = torch.zeros((n_inst, nt, 1), dtype=torch.complex128, device=dev)
+    E = d["E"][None, :]
+    stream = torch.cuda.current_stream(dev)
+
+    def once():
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        obs = batch.forward(E, d["gamma"])
+        e1.record(stream)
+        g = 2.0 * (obs - target)
+        batch.backward(g)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), e1.elapsed_time(e2)
+    for _ in range(max(1, min(args.warmup, 2))):
+        once()
+    fw, bw = [], []
+    for _ in range(max(1, min(args.steps, 3))):
+        a, b = once()
+        fw.append(a)
+        bw.append(b)
+    f, b = float(np.mean(fw)), float(np.mean(bw))
+    flops = 64 * 3 * 64 ** 3 * n_inst * nt
+    return dict(workload="driven%d" % n_inst, n_inst=n_inst, N=64, K=2, nt=nt, checkpoint_every=45,
+                fwd_ms=f, bwd_ms=b, bwd_over_fwd=b / f,
+                fwd_instance_steps_per_s=n_inst * nt / (f / 1e3),
+                fwd_tflops=flops / (f / 1e3) / 1e12,
+                note="fwd: FP32 CTA kernel with checkpoints; bwd: recompute + costate kernel "
+                     "(includes the gradient contractions); targets zero")
 
 
 # ---------------------------------------------------------------------------
@@ -396,6 +445,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16)
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--acc-sample", type=int, default=4)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adj-n-inst", type=int, default=256)
+    ap.add_argument("--adj-nt", type=int, default=2000)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
