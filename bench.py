@@ -446,11 +446,19 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--acc-sample", type=int, default=4)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--only-adjoint", action="store_true",
+                    help="time only the adjoint (fwd + bwd) on the driven workload")
     ap.add_argument("--adj-n-inst", type=int, default=256)
     ap.add_argument("--adj-nt", type=int, default=2000)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.only_adjoint:
+        import torch
+        from pyqed_gb300.build import build
+        build()
+        print(json.dumps(dict(adjoint=measure_adjoint(args, torch.device("cuda", 0)))))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if world > 1:
