@@ -163,7 +163,7 @@ def run_gpu(args):
         prop = new_prop(prec)
         prop.set_operators(bi.H, bi.cops, bi.eops, bi.dops)
         rho0_dev = prop.to_device(bi.rho0)
-        out = prop.alloc_outputs(want_obs=True, want_rho=False)
+        out = prop.alloc_outputs(want_obs=True, want_rho=True)
         stream = torch.cuda.current_stream(dev)
         for _ in range(args.warmup):
             prop.propagate_device(rho0_dev, drive_dev, out)
@@ -189,7 +189,8 @@ def run_gpu(args):
         info = prop.info()
         t = float(np.mean(times))
         results[prec] = dict(sec_per_step=t, times=times, wall=wall, info=info, clocks=clk,
-                             obs=prop.unpack_obs(out[0]) if out[0] is not None else None)
+                             obs=prop.unpack_obs(out[0]) if out[0] is not None else None,
+                             rho=out[1].cpu().numpy(), off=prop.off)
         prop.close()
 
     # ---- end to end through the public batched API (host buffers) ---------------
@@ -387,10 +388,19 @@ def cpu_baseline_and_accuracy(wl, results, args, chosen):
         pick = _sample_indices(wl["bi"].dims, args.acc_sample)
         acc = {}
         refs = {b: O.propagate_diag_correlation(ex["H"][b], ex["mu"][b], ex["rho_g"][b],
-                                                ex["c_diag"][b], ex["dt"], wl["nt"]) for b in pick}
+                                                ex["c_diag"][b], ex["dt"], wl["nt"],
+                                                return_rho=True) for b in pick}
         for prec, r in results.items():
-            errs = [np.abs(r["obs"][b, :, 0] - refs[b]).max() / np.abs(refs[b]).max() for b in pick]
-            acc[prec] = dict(max_rel_err_C=float(max(errs)), instances=pick, nt=wl["nt"])
+            errs = [np.abs(r["obs"][b, :, 0] - refs[b][0]).max() / np.abs(refs[b][0]).max()
+                    for b in pick]
+            rerr = []
+            for b in pick:
+                N = int(wl["bi"].dims[b])
+                got = r["rho"][r["off"][b]:r["off"][b + 1]].reshape(N, N)
+                rerr.append(np.abs(got - refs[b][1]).max())
+            acc[prec] = dict(max_rel_err_C=float(max(errs)), max_abs_err_rho_final=float(max(rerr)),
+                             instances=pick, nt=wl["nt"],
+                             reference="complex128 oracle (pyqed/oqs.py:717-791 recurrence)")
     del multiprocessing
     return cb, acc
 

@@ -180,17 +180,18 @@ def rhs_diag(rho, H, c_diag):
     return -1j * (Heff @ rho - rho @ Heff.conj().T) + D * rho
 
 
-def propagate_diag_correlation(H, mu, rho_g, c_diag, dt, Nt):
+def propagate_diag_correlation(H, mu, rho_g, c_diag, dt, Nt, return_rho=False):
     """C_k = Tr[mu rho(t_k)], rho(0) = mu rho_g, diagonal collapse operators.
 
-    Same recurrence as ``correlation_2op_1t`` with A = B = mu.
+    Same recurrence as ``correlation_2op_1t`` with A = B = mu.  With
+    ``return_rho`` the final rho(t_Nt) is returned as well.
     """
     rho = mu @ rho_g
     cor = np.zeros(Nt, dtype=complex)
     for k in range(Nt):
         rho = rk4_step(rho, dt, H, c_diag, f=rhs_diag)
         cor[k] = obs_dm(rho, mu)
-    return cor
+    return (cor, rho) if return_rho else cor
 
 
 def liouvillian_superop(H, c_ops):
