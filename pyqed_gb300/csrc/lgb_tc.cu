@@ -19,10 +19,10 @@
 //   X A^dag:   P = -i X  (rows (Xi, -Xr) of the XM buffer),  Q = i A^dag  (the same A
 //              buffer read as the N side: part 0 = Ai, part 1 = Ar)
 // so one A buffer serves both products.  Every operand is split into hi + lo
-// (TF32 or BF16) and each product keeps the three leading terms; the hi/lo
-// pair of the N-side operand is concatenated along N (hi columns 0..2NP-1,
-// lo columns 2NP..4NP-1), so a stage is 4 K-loops of NP/kK instructions at
-// N = 4NP or 2NP (32 instructions at NP = 64 for TF32) and one commit.
+// (TF32 or BF16) and each product keeps the three leading terms, so a stage
+// is 6 K-loops of NP/kK instructions at N = 2NP (48 instructions at NP = 64
+// for TF32, against 96 at N = NP for the Re/Im-blocked embedding) into one
+// accumulator, and one commit.
 //
 // Each of the 512 threads owns a quarter of the columns of one TMEM lane (one
 // component of one row); it keeps rho, the RK4 sum, a Kahan compensation term
@@ -34,6 +34,8 @@
 // bounded; a wait that runs out marks the instance LGB_ERR_TIMEOUT and the CTA
 // stops.
 #include <cuda_bf16.h>
+
+#include <type_traits>
 
 #include "lgb_common.cuh"
 #include "lgb_internal.h"
@@ -48,7 +50,7 @@ using namespace umma;
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxEops = 16;
-constexpr uint32_t kTmemCols = 256;  // D: 4 NP <= 256 columns
+constexpr uint32_t kTmemCols = 128;  // D: 2 NP <= 128 columns
 
 // TF32 or BF16 operand element
 template <bool BF16> struct Elem;
@@ -88,10 +90,10 @@ struct TcShared {
 //   groups SBO_T apart, SBO_T = 32 mod 64 B, so that the column-wise scalar
 //   stores of a warp (16 rows i of each of two row halves, 2 row groups
 //   apart) hit distinct banks.
-// Each buffer holds the hi level (2 NP rows) followed by the lo level, so
-// [hi ; lo] is one N-side operand of 4 NP rows.  An M-side operand reads 128
-// rows from its level base; the rows past 2 NP belong to lanes no thread uses
-// and stay inside the buffer (BYTES covers the last window).
+// Each buffer holds the hi level (2 NP rows) followed by the lo level.  An
+// M-side operand reads 128 rows from its level base; the rows past 2 NP belong
+// to lanes no thread uses and stay inside the buffer (BYTES covers the last
+// window).
 template <bool BF16, int NP>
 struct Geo {
   static constexpr int EPC = 16 / Elem<BF16>::kSize;  // elements per 16 bytes
@@ -145,31 +147,35 @@ __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t
 // descriptor for base + off is the base descriptor + (off >> 4).
 __device__ __forceinline__ uint64_t dadd(uint64_t d, uint32_t off) { return d + (off >> 4); }
 
-// The 4 K-loops of one RK4 stage (single issuing thread).
+// The 6 K-loops of one RK4 stage (single issuing thread), all at N = 2 NP
+// into one accumulator.
 template <bool BF16, int NP>
 __device__ __forceinline__ void issue_stage(uint32_t d, uint32_t base) {
   using G = Geo<BF16, NP>;
-  constexpr uint32_t id2 = idesc(Elem<BF16>::kFmt, 128, 2 * NP, false, false);
-  constexpr uint32_t id4 = idesc(Elem<BF16>::kFmt, 128, 4 * NP, false, false);
+  constexpr uint32_t id = idesc(Elem<BF16>::kFmt, 128, 2 * NP, false, false);
   const uint64_t dA = sdesc(base + G::OFF_A, 128, G::SBO_S);
   const uint64_t dXM = sdesc(base + G::OFF_XM, 128, G::SBO_S);
   const uint64_t dXT = sdesc(base + G::OFF_XT, G::LBO_T, G::SBO_T);
-  // A_hi . [X_hi | X_lo]
+  // A X: A_hi X_hi, A_hi X_lo, A_lo X_hi
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dA, s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id4, s > 0 ? 1u : 0u);
-  // A_lo . X_hi
+    mma<BF16>(d, dadd(dA, s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, s > 0 ? 1u : 0u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dA, G::LVL_S + s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id2, 1u);
-  // (-i X_hi) . [i A_hi^dag | i A_lo^dag]
+    mma<BF16>(d, dadd(dA, s * G::KSTEP_S), dadd(dXT, G::LVL_T + s * G::KSTEP_T), id, 1u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dXM, s * G::KSTEP_S), dadd(dA, s * G::KSTEP_S), id4, 1u);
-  // (-i X_lo) . i A_hi^dag
+    mma<BF16>(d, dadd(dA, G::LVL_S + s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, 1u);
+  // X A^dag = (-i X) (i A^dag): X_hi A_hi, X_hi A_lo, X_lo A_hi
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dXM, G::LVL_S + s * G::KSTEP_S), dadd(dA, s * G::KSTEP_S), id2, 1u);
+    mma<BF16>(d, dadd(dXM, s * G::KSTEP_S), dadd(dA, s * G::KSTEP_S), id, 1u);
+#pragma unroll
+  for (int s = 0; s < G::KS; ++s)
+    mma<BF16>(d, dadd(dXM, s * G::KSTEP_S), dadd(dA, G::LVL_S + s * G::KSTEP_S), id, 1u);
+#pragma unroll
+  for (int s = 0; s < G::KS; ++s)
+    mma<BF16>(d, dadd(dXM, G::LVL_S + s * G::KSTEP_S), dadd(dA, s * G::KSTEP_S), id, 1u);
 }
 
 __device__ __forceinline__ void sync_for_mma() {
@@ -254,28 +260,42 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     }
   };
 
-  // ---- X operands of the stage input x (this thread's component of row i):
+  // ---- X operands of a stage input x (this thread's component of row i):
   //   XM (M side of X A^dag): row (0, i) = Xi[i], row (1, i) = -Xr[i]
   //   X^T (N side of A X):    row (0, j) = Xr[.][j], row (1, j) = Xi[.][j], K index i
+  // written 4 columns at a time (group g: columns j0 + 4g .. j0 + 4g + 3).
   const int xm_row = mrow(1 - c, i);
   const float xm_sign = c == 0 ? -1.f : 1.f;
-  auto write_x = [&](const float* x) {
+  auto write_group = [&](int g, const float* x4) {
     if (!row_ok) return;
+    float vh[4], vl[4];
 #pragma unroll
-    for (int g = 0; g < NG; ++g) {
-      float vh[4], vl[4];
+    for (int e = 0; e < 4; ++e) El::split(x4[e], vh[e], vl[e]);  // split(-x) = -split(x)
+    const int col = j0 + g * 4;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) El::split(xm_sign * x[g * 4 + e], vh[e], vl[e]);
-      const int col = j0 + g * 4;
-      st4<BF16>(SXM + off_s<BF16, NP>(xm_row, col), vh);
-      st4<BF16>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col), vl);
+    for (int e = 0; e < 4; ++e) {
+      const uint32_t o = off_t<BF16, NP>(ncol(c, col + e), i);
+      *reinterpret_cast<ET*>(SXT + o) = (ET)vh[e];
+      *reinterpret_cast<ET*>(SXT + G::LVL_T + o) = (ET)vl[e];
+      vh[e] *= xm_sign;
+      vl[e] *= xm_sign;
+    }
+    st4<BF16>(SXM + off_s<BF16, NP>(xm_row, col), vh);
+    st4<BF16>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col), vl);
+  };
+  // hi + lo of the current stage input of group g, read back from XM (used by
+  // the general diagonal dissipator)
+  auto read_group = [&](int g, float* x4) {
+    const int col = j0 + g * 4;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const uint32_t o = off_t<BF16, NP>(ncol(c, col + e), i);
-        // the sign flip of the XM copy is undone for X^T (exact)
-        *reinterpret_cast<ET*>(SXT + o) = (ET)(xm_sign * vh[e]);
-        *reinterpret_cast<ET*>(SXT + G::LVL_T + o) = (ET)(xm_sign * vl[e]);
+    for (int e = 0; e < 4; ++e) {
+      float v = 0.f;
+      if (row_ok) {
+        const uint32_t o = off_s<BF16, NP>(xm_row, col + e);
+        v = (float)*reinterpret_cast<const ET*>(SXM + o) +
+            (float)*reinterpret_cast<const ET*>(SXM + G::LVL_S + o);
       }
+      x4[e] = xm_sign * v;
     }
   };
 
@@ -366,7 +386,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   };
 
   // ---- state -------------------------------------------------------------------
-  float rho[NPQ], racc[NPQ], kc[NPQ], xin[NPQ];
+  float rho[NPQ], racc[NPQ], kc[NPQ];
   {
     const double2* r0 = p.rho0 + p.off[b];
 #pragma unroll
@@ -378,7 +398,6 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         v = c == 0 ? z.x : z.y;
       }
       rho[jj] = (float)v;
-      xin[jj] = rho[jj];
       racc[jj] = 0.f;
       kc[jj] = 0.f;
     }
@@ -402,7 +421,13 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const bool dfast = diag && !dgeneral && !dcomplex;
   const int dpos = (i >= j0 && i < j0 + NPQ) ? i - j0 : -1;
   const float dd = (dfast && dpos >= 0 && i < N) ? Dm[i * NPS + i].x : 0.f;
+  // diagonal element (i, i) of the stage input, for the dfast dissipator
+  float xd = 0.f;
+#pragma unroll
+  for (int jj = 0; jj < NPQ; ++jj) xd = (jj == dpos) ? rho[jj] : xd;
   if (p.n_drive == 0) build_a(nullptr);
+#pragma unroll
+  for (int g = 0; g < NG; ++g) write_group(g, rho + g * 4);
   if (tid == 0) p.err[b] = 0;
   if (p.obs_t0) obs_finish(obs_partials(rho), 0);
   // The observables of step s are reduced while the MMAs of the first stage
@@ -422,7 +447,6 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     }
 #pragma unroll 1
     for (int stage = 0; stage < 4; ++stage) {
-      write_x(xin);
       sync_for_mma();
       if (tid == 0) {
         fence_after_sync();
@@ -442,49 +466,68 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       fence_after_sync();
       // RHS element R = (combined accumulator) + (D o X); stages 0-2 form the
       // RK4 sum and the next stage input, stage 3 applies the Kahan-compensated
-      // update.  Columns in groups of 4 (a group never crosses a 16-block).
+      // update.  Each group of 4 columns (never crossing a 16-block) is loaded
+      // from TMEM, combined with the partner lane, updated and written straight
+      // into the operand buffers of the next stage.
+      const float cst = (stage == 2) ? dt : half_dt;
+      const float keep = (stage == 0) ? 0.f : 1.f;
+      const float w = (stage == 0) ? 1.f : 2.f;
+      // MODE 0: no dissipator, 1: pure dephasing (diagonal real D), 2: general
+      // diagonal D; LAST: stage 3.  The branches are resolved outside the
+      // unrolled element loops.
+      auto epilogue = [&](auto mode_tag, auto last_tag) {
+        constexpr int MODE = decltype(mode_tag)::value;
+        constexpr bool LAST = decltype(last_tag)::value;
+        const float sg = c == 0 ? -1.f : 1.f;
 #pragma unroll
-      for (int g = 0; g < NG; ++g) {
-        const int col = j0 + g * 4;
-        const uint32_t n1 = (uint32_t)ncol(1, col), n0 = (uint32_t)ncol(0, col);
-        float a1[4], a0[4], b1[4], b0[4];
-        tmem_ld4(tlane + n1, a1);
-        tmem_ld4(tlane + n0, a0);
-        tmem_ld4(tlane + 2 * NP + n1, b1);
-        tmem_ld4(tlane + 2 * NP + n0, b0);
-        tmem_wait_ld();
+        for (int g = 0; g < NG; ++g) {
+          const int col = j0 + g * 4;
+          float a1[4], a0[4], xo[4], xn[4];
+          tmem_ld4(tlane + (uint32_t)ncol(1, col), a1);
+          tmem_ld4(tlane + (uint32_t)ncol(0, col), a0);
+          if constexpr (MODE == 2) read_group(g, xo);
+          tmem_wait_ld();
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int jj = g * 4 + e;
-          const float q1 = a1[e] + b1[e];
-          const float q0 = a0[e] + b0[e];
-          const float q1x = __shfl_xor_sync(0xffffffffu, q1, 16);
-          float R = c == 0 ? q0 - q1x : q0 + q1x;
-          if (dfast) {
-            R = (jj == dpos) ? fmaf(dd, xin[jj], R) : R;
-          } else if (diag) {
-            const float xo = dcomplex ? __shfl_xor_sync(0xffffffffu, xin[jj], 16) : 0.f;
-            if (row_ok) {
-              const float2 d = Dm[i * NPS + j0 + jj];
-              R = fmaf(d.x, xin[jj], R);
-              if (dcomplex) R = fmaf(c == 0 ? -d.y : d.y, xo, R);
+          for (int e = 0; e < 4; ++e) {
+            const int jj = g * 4 + e;
+            const float q1x = __shfl_xor_sync(0xffffffffu, a1[e], 16);
+            float R = fmaf(sg, q1x, a0[e]);
+            if constexpr (MODE == 1) {
+              R = (jj == dpos) ? fmaf(dd, xd, R) : R;
+            } else if constexpr (MODE == 2) {
+              const float xp = dcomplex ? __shfl_xor_sync(0xffffffffu, xo[e], 16) : 0.f;
+              if (row_ok) {
+                const float2 d = Dm[i * NPS + col + e];
+                R = fmaf(d.x, xo[e], R);
+                if (dcomplex) R = fmaf(sg * d.y, xp, R);
+              }
             }
+            if constexpr (!LAST) {
+              racc[jj] = fmaf(w, R, keep * racc[jj]);
+              xn[e] = fmaf(cst, R, rho[jj]);
+            } else {
+              // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4)
+              const float y = fmaf(sixth_dt, racc[jj] + R, -kc[jj]);
+              const float t = rho[jj] + y;
+              kc[jj] = (t - rho[jj]) - y;
+              rho[jj] = t;
+              xn[e] = t;
+            }
+            if constexpr (MODE == 1) xd = (jj == dpos) ? xn[e] : xd;
           }
-          if (stage < 3) {
-            const float cst = (stage == 2) ? dt : half_dt;
-            const float keep = (stage == 0) ? 0.f : 1.f;
-            const float w = (stage == 0) ? 1.f : 2.f;
-            racc[jj] = fmaf(w, R, keep * racc[jj]);
-            xin[jj] = fmaf(cst, R, rho[jj]);
-          } else {
-            // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4)
-            const float y = fmaf(sixth_dt, racc[jj] + R, -kc[jj]);
-            const float t = rho[jj] + y;
-            kc[jj] = (t - rho[jj]) - y;
-            rho[jj] = t;
-            xin[jj] = t;
-          }
+          write_group(g, xn);
         }
+      };
+      using F = std::false_type;
+      using T = std::true_type;
+      if (stage < 3) {
+        if (!diag) epilogue(std::integral_constant<int, 0>{}, F{});
+        else if (dfast) epilogue(std::integral_constant<int, 1>{}, F{});
+        else epilogue(std::integral_constant<int, 2>{}, F{});
+      } else {
+        if (!diag) epilogue(std::integral_constant<int, 0>{}, T{});
+        else if (dfast) epilogue(std::integral_constant<int, 1>{}, T{});
+        else epilogue(std::integral_constant<int, 2>{}, T{});
       }
     }
     if (!alive || nonfinite) break;
