@@ -299,6 +299,12 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     }
   };
 
+  // ---- state: element jj of this thread is component .x (jj even) or .y (jj
+  // odd) of pair jj / 2, so the RK4 arithmetic runs on packed FP32x2 pairs;
+  // nkc holds the negated Kahan compensation.
+  float2 rho2[NPQ / 2], racc2[NPQ / 2], nkc2[NPQ / 2];
+  auto rho_at = [&](int jj) -> float { return (jj & 1) ? rho2[jj >> 1].y : rho2[jj >> 1].x; };
+
   // ---- observables Tr[O rho]: FP32 partials per thread and warp (pairwise
   // shuffle tree), folded across warps by a second shuffle tree and written in
   // FP64.  A per-thread mask skips the zero entries of O (sparse observables
@@ -317,11 +323,11 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   }
   // Part 1 (no barrier): per-warp partials of every Tr[O_e rho] into sh.red;
   // returns whether this thread's elements are finite.
-  auto obs_partials = [&](const float* rho) -> bool {
+  auto obs_partials = [&]() -> bool {
     bool fin = true;
     if (i < N) {
 #pragma unroll
-      for (int jj = 0; jj < NPQ; ++jj) fin = fin && isfinite(rho[jj]);
+      for (int jj = 0; jj < NPQ; ++jj) fin = fin && isfinite(rho_at(jj));
     }
     for (int e = 0; e < E; ++e) {
       float fx = 0.f, fy = 0.f;
@@ -336,11 +342,11 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
 #pragma unroll
         for (int jj = 0; jj < NPQ; ++jj) {
           if (c == 0) {
-            fx = fmaf(ov[jj].x, rho[jj], fx);
-            fy = fmaf(ov[jj].y, rho[jj], fy);
+            fx = fmaf(ov[jj].x, rho_at(jj), fx);
+            fy = fmaf(ov[jj].y, rho_at(jj), fy);
           } else {
-            fx = fmaf(-ov[jj].y, rho[jj], fx);
-            fy = fmaf(ov[jj].x, rho[jj], fy);
+            fx = fmaf(-ov[jj].y, rho_at(jj), fx);
+            fy = fmaf(ov[jj].x, rho_at(jj), fy);
           }
         }
       }
@@ -386,7 +392,6 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   };
 
   // ---- state -------------------------------------------------------------------
-  float rho[NPQ], racc[NPQ], kc[NPQ];
   {
     const double2* r0 = p.rho0 + p.off[b];
 #pragma unroll
@@ -397,9 +402,13 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         const double2 z = r0[(long long)i * N + j];
         v = c == 0 ? z.x : z.y;
       }
-      rho[jj] = (float)v;
-      racc[jj] = 0.f;
-      kc[jj] = 0.f;
+      if (jj & 1) {
+        rho2[jj >> 1].y = (float)v;
+      } else {
+        rho2[jj >> 1].x = (float)v;
+        racc2[jj >> 1] = make_float2(0.f, 0.f);
+        nkc2[jj >> 1] = make_float2(0.f, 0.f);
+      }
     }
   }
 
@@ -421,15 +430,19 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const bool dfast = diag && !dgeneral && !dcomplex;
   const int dpos = (i >= j0 && i < j0 + NPQ) ? i - j0 : -1;
   const float dd = (dfast && dpos >= 0 && i < N) ? Dm[i * NPS + i].x : 0.f;
-  // diagonal element (i, i) of the stage input, for the dfast dissipator
+  // warps that hold diagonal elements; element (i, i) of the stage input
+  const bool dwarp = __any_sync(0xffffffffu, dpos >= 0 && i < N) != 0;
   float xd = 0.f;
 #pragma unroll
-  for (int jj = 0; jj < NPQ; ++jj) xd = (jj == dpos) ? rho[jj] : xd;
+  for (int jj = 0; jj < NPQ; ++jj) xd = (jj == dpos) ? rho_at(jj) : xd;
   if (p.n_drive == 0) build_a(nullptr);
 #pragma unroll
-  for (int g = 0; g < NG; ++g) write_group(g, rho + g * 4);
+  for (int g = 0; g < NG; ++g) {
+    const float x4[4] = {rho2[2 * g].x, rho2[2 * g].y, rho2[2 * g + 1].x, rho2[2 * g + 1].y};
+    write_group(g, x4);
+  }
   if (tid == 0) p.err[b] = 0;
-  if (p.obs_t0) obs_finish(obs_partials(rho), 0);
+  if (p.obs_t0) obs_finish(obs_partials(), 0);
   // The observables of step s are reduced while the MMAs of the first stage
   // of step s + 1 run (and after the loop for the last step).
   int pend_row = -1;
@@ -453,7 +466,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         issue_stage<BF16, NP>(sh.tmem_base, sbase);
         mma_commit(&sh.mbar);
       }
-      if (stage == 0 && pend_row >= 0) pend_fin = obs_partials(rho);
+      if (stage == 0 && pend_row >= 0) pend_fin = obs_partials();
       if (!wait_mma()) break;
       if (stage == 0 && pend_row >= 0) {
         const bool bad = obs_finish(pend_fin, pend_row);
@@ -469,66 +482,85 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       // update.  Each group of 4 columns (never crossing a 16-block) is loaded
       // from TMEM, combined with the partner lane, updated and written straight
       // into the operand buffers of the next stage.
-      const float cst = (stage == 2) ? dt : half_dt;
-      const float keep = (stage == 0) ? 0.f : 1.f;
-      const float w = (stage == 0) ? 1.f : 2.f;
-      // MODE 0: no dissipator, 1: pure dephasing (diagonal real D), 2: general
-      // diagonal D; LAST: stage 3.  The branches are resolved outside the
-      // unrolled element loops.
-      auto epilogue = [&](auto mode_tag, auto last_tag) {
+      const float2 cst2 = make_float2(stage == 2 ? dt : half_dt, stage == 2 ? dt : half_dt);
+      // MODE 0: no diagonal dissipator term in this warp, 1: pure dephasing
+      // (diagonal real D) in a warp that holds diagonal elements, 2: general
+      // diagonal D.  STAGE 0, 1 (stages 1 and 2) or 3.  Mode and stage are
+      // resolved outside the unrolled element loops.
+      auto epilogue = [&](auto mode_tag, auto stage_tag) {
         constexpr int MODE = decltype(mode_tag)::value;
-        constexpr bool LAST = decltype(last_tag)::value;
+        constexpr int STAGE = decltype(stage_tag)::value;
         const float sg = c == 0 ? -1.f : 1.f;
+        const float2 sg2 = make_float2(sg, sg), m1 = make_float2(-1.f, -1.f);
+        const float ddxd = dd * xd;
 #pragma unroll
         for (int g = 0; g < NG; ++g) {
           const int col = j0 + g * 4;
-          float a1[4], a0[4], xo[4], xn[4];
+          float a1[4], a0[4], xo[4];
           tmem_ld4(tlane + (uint32_t)ncol(1, col), a1);
           tmem_ld4(tlane + (uint32_t)ncol(0, col), a0);
           if constexpr (MODE == 2) read_group(g, xo);
           tmem_wait_ld();
+          float q1x[4];
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int jj = g * 4 + e;
-            const float q1x = __shfl_xor_sync(0xffffffffu, a1[e], 16);
-            float R = fmaf(sg, q1x, a0[e]);
+          for (int e = 0; e < 4; ++e) q1x[e] = __shfl_xor_sync(0xffffffffu, a1[e], 16);
+          float2 xn2[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int k = 2 * g + h;  // pair index
+            float2 R = __ffma2_rn(sg2, make_float2(q1x[2 * h], q1x[2 * h + 1]),
+                                  make_float2(a0[2 * h], a0[2 * h + 1]));
             if constexpr (MODE == 1) {
-              R = (jj == dpos) ? fmaf(dd, xd, R) : R;
+              R = __fadd2_rn(R, make_float2(2 * k == dpos ? ddxd : 0.f, 2 * k + 1 == dpos ? ddxd : 0.f));
             } else if constexpr (MODE == 2) {
-              const float xp = dcomplex ? __shfl_xor_sync(0xffffffffu, xo[e], 16) : 0.f;
-              if (row_ok) {
-                const float2 d = Dm[i * NPS + col + e];
-                R = fmaf(d.x, xo[e], R);
-                if (dcomplex) R = fmaf(sg * d.y, xp, R);
+#pragma unroll
+              for (int u = 0; u < 2; ++u) {
+                const int e = 2 * h + u;
+                const float xp = dcomplex ? __shfl_xor_sync(0xffffffffu, xo[e], 16) : 0.f;
+                float r = u ? R.y : R.x;
+                if (row_ok) {
+                  const float2 d = Dm[i * NPS + col + e];
+                  r = fmaf(d.x, xo[e], r);
+                  if (dcomplex) r = fmaf(sg * d.y, xp, r);
+                }
+                if (u) R.y = r; else R.x = r;
               }
             }
-            if constexpr (!LAST) {
-              racc[jj] = fmaf(w, R, keep * racc[jj]);
-              xn[e] = fmaf(cst, R, rho[jj]);
+            if constexpr (STAGE == 0) {
+              racc2[k] = R;
+              xn2[h] = __ffma2_rn(cst2, R, rho2[k]);
+            } else if constexpr (STAGE == 1) {
+              racc2[k] = __ffma2_rn(make_float2(2.f, 2.f), R, racc2[k]);
+              xn2[h] = __ffma2_rn(cst2, R, rho2[k]);
             } else {
               // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4)
-              const float y = fmaf(sixth_dt, racc[jj] + R, -kc[jj]);
-              const float t = rho[jj] + y;
-              kc[jj] = (t - rho[jj]) - y;
-              rho[jj] = t;
-              xn[e] = t;
+              const float2 y = __ffma2_rn(make_float2(sixth_dt, sixth_dt), __fadd2_rn(racc2[k], R), nkc2[k]);
+              const float2 t = __fadd2_rn(rho2[k], y);
+              nkc2[k] = __ffma2_rn(__ffma2_rn(rho2[k], m1, t), m1, y);  // y - (t - rho)
+              rho2[k] = t;
+              xn2[h] = t;
             }
-            if constexpr (MODE == 1) xd = (jj == dpos) ? xn[e] : xd;
+            if constexpr (MODE == 1) {
+              xd = (2 * k == dpos) ? xn2[h].x : xd;
+              xd = (2 * k + 1 == dpos) ? xn2[h].y : xd;
+            }
           }
-          write_group(g, xn);
+          const float x4[4] = {xn2[0].x, xn2[0].y, xn2[1].x, xn2[1].y};
+          write_group(g, x4);
         }
       };
-      using F = std::false_type;
-      using T = std::true_type;
-      if (stage < 3) {
-        if (!diag) epilogue(std::integral_constant<int, 0>{}, F{});
-        else if (dfast) epilogue(std::integral_constant<int, 1>{}, F{});
-        else epilogue(std::integral_constant<int, 2>{}, F{});
-      } else {
-        if (!diag) epilogue(std::integral_constant<int, 0>{}, T{});
-        else if (dfast) epilogue(std::integral_constant<int, 1>{}, T{});
-        else epilogue(std::integral_constant<int, 2>{}, T{});
-      }
+      using S0 = std::integral_constant<int, 0>;
+      using S1 = std::integral_constant<int, 1>;
+      using S3 = std::integral_constant<int, 3>;
+      const int mode = !diag ? 0 : (dfast ? (dwarp ? 1 : 0) : 2);
+      auto by_mode = [&](auto stage_tag) {
+        if (mode == 0) epilogue(std::integral_constant<int, 0>{}, stage_tag);
+        else if (mode == 1) epilogue(std::integral_constant<int, 1>{}, stage_tag);
+        else epilogue(std::integral_constant<int, 2>{}, stage_tag);
+      };
+      if (stage == 0) by_mode(S0{});
+      else if (stage < 3) by_mode(S1{});
+      else by_mode(S3{});
     }
     if (!alive || nonfinite) break;
     pend_row = step + p.obs_t0;
@@ -539,19 +571,19 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
 #pragma unroll
       for (int jj = 0; jj < NPQ; ++jj) {
         const int j = j0 + jj;
-        if (j < N) reinterpret_cast<double*>(dst + (long long)i * N + j)[c] = (double)rho[jj];
+        if (j < N) reinterpret_cast<double*>(dst + (long long)i * N + j)[c] = (double)rho_at(jj);
       }
     }
   }
 
-  if (alive && !nonfinite && pend_row >= 0) nonfinite = obs_finish(obs_partials(rho), pend_row);
+  if (alive && !nonfinite && pend_row >= 0) nonfinite = obs_finish(obs_partials(), pend_row);
   if (nonfinite && tid == 0) p.err[b] = 4;  // LGB_ERR_NONFINITE
   if (alive && p.rho_out != nullptr && i < N) {
     double2* dst = p.rho_out + p.off[b];
 #pragma unroll
     for (int jj = 0; jj < NPQ; ++jj) {
       const int j = j0 + jj;
-      if (j < N) reinterpret_cast<double*>(dst + (long long)i * N + j)[c] = (double)rho[jj];
+      if (j < N) reinterpret_cast<double*>(dst + (long long)i * N + j)[c] = (double)rho_at(jj);
     }
   }
   // TMEM reads of this instance are done before the next instance's first MMA
