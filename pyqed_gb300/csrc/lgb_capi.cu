@@ -209,10 +209,6 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
     delete pl;
     return LGB_ERR_UNSUPPORTED;
   }
-  if (sched == LGB_SCHED_GEMM && (prec == LGB_PREC_TF32X3 || prec == LGB_PREC_BF16X3)) {
-    delete pl;
-    return LGB_ERR_UNSUPPORTED;
-  }
   pl->schedule = sched;
   pl->smem_bytes = smem;
   pl->smem_w = smem_w;
@@ -291,7 +287,9 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
     for (int b = 0; b < n; ++b) maxn = std::max(maxn, pl->dims[b]);
     double2* partial = nullptr;
     int* counter = nullptr;
-    s = s ? s : dalloc(pl, &partial, (size_t)std::max(E, 1) * lgb::gemm_partial_slots(maxn) * sizeof(double2));
+    const size_t slots = split ? std::max(lgb::gemm_partial_slots(maxn), lgb::split_partial_slots(maxn))
+                               : lgb::gemm_partial_slots(maxn);
+    s = s ? s : dalloc(pl, &partial, (size_t)std::max(E, 1) * slots * sizeof(double2));
     s = s ? s : dalloc(pl, &counter, sizeof(int));
     if (s == LGB_OK) s = cuda_status(cudaMemset(counter, 0, sizeof(int)));
     s = s ? s : dalloc(pl, &pl->d_gtmp, dense ? (size_t)maxn * maxn * sizeof(double2) : 0);
@@ -314,6 +312,26 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
       g.partial = partial;
       g.counter = counter;
       g.err = pl->d_err + b;
+    }
+    if (split) {
+      // split operands: interleaved hi/lo arrays padded to NP = 128 k
+      const bool bf16 = prec == LGB_PREC_BF16X3;
+      const size_t ses = bf16 ? 2 : 4;
+      pl->gsplit.resize(n);
+      for (int b = 0; b < n && s == LGB_OK; ++b) {
+        lgb::GemmSplit& q = pl->gsplit[b];
+        q.NP = lgb::split_padded_dim(pl->dims[b]);
+        q.Wp = (long long)(Kd + 2) * q.NP;
+        q.bf16 = bf16;
+        for (int l = 0; l < 2; ++l) {
+          s = s ? s : dalloc(pl, &q.Ls[l], (size_t)2 * q.NP * q.Wp * ses);
+          s = s ? s : dalloc(pl, &q.Rs[l], (size_t)2 * q.NP * q.Wp * ses);
+          s = s ? s : dalloc(pl, &q.Lks[l], (size_t)Kd * 2 * q.NP * q.NP * ses);
+        }
+        s = s ? s : dalloc(pl, &q.Tpart, Kd ? lgb::split_tpart_elems(q.NP, Kd, pl->n_sm, bf16) * sizeof(float2) : 0);
+        s = s ? s : dalloc(pl, &q.Rpart, lgb::split_rpart_elems(q.NP, Kd, pl->n_sm, bf16) * sizeof(float2));
+        s = s ? s : dalloc(pl, &q.kc, (size_t)pl->dims[b] * pl->dims[b] * sizeof(float2));
+      }
     }
     if (s == LGB_OK) {
       if (cublasCreate(&pl->blas) != CUBLAS_STATUS_SUCCESS) {
@@ -396,6 +414,9 @@ int lgb_plan_set_operators(lgb_plan_t plan, const double* H, const double* cops,
       a.doff = 0;
       a.Gtmp = plan->d_gtmp;
       s = lgb::gemm_setup(a, st);
+      if (s == LGB_OK && !plan->gsplit.empty())
+        s = lgb::split_setup(plan->gsplit[b], plan->gemm[b], pr.cops_kind == LGB_COPS_DENSE ? K : 0,
+                             pr.precision == LGB_PREC_BF16X3, plan->n_sm, st);
     }
   } else {
     s = cuda_status(lgb::launch_setup(sp, pr.precision == LGB_PREC_FP64 ? 0 : 1, st));
@@ -459,6 +480,8 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
       a.g = plan->gemm[b];
       a.blas = plan->blas;
       a.fp64 = pr.precision == LGB_PREC_FP64;
+      a.split = !plan->gsplit.empty();
+      if (a.split) a.sp = plan->gsplit[b];
       a.Kdense = pr.cops_kind == LGB_COPS_DENSE ? pr.n_cops : 0;
       a.D = pr.n_drive;
       a.E = pr.n_eops;
@@ -634,12 +657,16 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
   info->launches_per_propagate = (plan->order.empty() ? 0 : 1) + (plan->order_w.empty() ? 0 : 1) +
                                  (plan->tc_order.empty() ? 0 : 1);
   if (plan->schedule == LGB_SCHED_GEMM) {
-    // per instance: init (+ t0 observables) + per step (drive) + 4 x (G1, G2, epilogue)
+    // per instance: init (+ t0 observables) + per step (drive) + 4 x (G1, G2, epilogue);
+    // split precision: init also converts X (2 kernels), the drive step also
+    // converts A and A^dag (2), and G1 has its split consumer
     const lgb_problem_t& pr = plan->prob;
-    const int per_stage = (pr.cops_kind == LGB_COPS_DENSE ? 2 : 1) + 1;
-    info->launches_per_propagate =
-        pr.n_inst * (1 + (pr.obs_t0 && pr.n_eops ? 1 : 0) +
-                     pr.nt * (4 * per_stage + (pr.n_drive > 0 ? 1 : 0)));
+    const bool split = !plan->gsplit.empty();
+    const bool dense = pr.cops_kind == LGB_COPS_DENSE;
+    const int per_stage = (dense ? (split ? 2 : 1) : 0) + 2;
+    const int per_drive = pr.n_drive > 0 ? (split ? 3 : 1) : 0;
+    const int init = 1 + (split ? 2 : 0) + (pr.obs_t0 && pr.n_eops ? 1 : 0);
+    info->launches_per_propagate = pr.n_inst * (init + pr.nt * (4 * per_stage + per_drive));
   }
   info->workspace_bytes = (int64_t)plan->ws_bytes;
   info->flops_per_step = plan->flops_per_step;

@@ -395,7 +395,20 @@ static int gemm_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
 }
 
 int gemm_propagate(const GemmRunArgs& a, cudaStream_t st) {
+  if (a.split) return split_propagate(a, st);
   return a.fp64 ? gemm_propagate_t<double>(a, st) : gemm_propagate_t<float>(a, st);
+}
+
+void gemm_init_split(const GemmInstance& g, const double2* rho0, cudaStream_t st) {
+  const long long NN = (long long)g.N * g.N;
+  gemm_init_kernel<float><<<(int)std::min<long long>((NN + 255) / 256, 4096), 256, 0, st>>>(g, rho0);
+}
+void gemm_obs_split(const GemmInstance& g, int E, double2* obs_out, cudaStream_t st) {
+  gemm_obs_kernel<float><<<epi_grid(g.N), kEpiThreads, 0, st>>>(g, E, obs_out, 0);
+}
+void gemm_drive_split(const GemmInstance& g, int D, const double* f, int nt, int step, cudaStream_t st) {
+  const long long NN = (long long)g.N * g.N;
+  gemm_drive_kernel<float><<<(int)std::min<long long>((NN + 255) / 256, 4096), 256, 0, st>>>(g, D, f, nt, step);
 }
 
 }  // namespace lgb

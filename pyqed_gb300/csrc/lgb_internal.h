@@ -1,6 +1,7 @@
 // Internal plan structure and kernel launchers shared by the C-ABI layer.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -107,8 +108,28 @@ struct GemmSetupArgs {
   long long doff = 0;             // packed-diagonal base of this instance (diag kind)
   double2* Gtmp = nullptr;        // N x N FP64 scratch for sum_k L_k^dag L_k
 };
+// Split-precision operands of the GEMM schedule (lgb_gemm_tc.cu): the
+// interleaved K-major hi/lo arrays of G2 (Ls: M side [A | X | T_k], Rs: N side
+// [X ; A^dag ; L_k^dag] transposed) and of G1 (Lks: the L_k), the split-K
+// partial outputs, the Kahan compensation and the TMA tensor maps.
+struct GemmSplit {
+  int NP = 0;                    // dimension padded to a multiple of 128
+  long long Wp = 0;              // (K_dense + 2) NP, the K extent of G2
+  bool bf16 = false;
+  void* Ls[2] = {nullptr, nullptr};   // 2 NP x Wp
+  void* Rs[2] = {nullptr, nullptr};   // 2 NP x Wp
+  void* Lks[2] = {nullptr, nullptr};  // K x 2 NP x NP
+  float2* Tpart = nullptr;       // ks1 x K x NP x NP
+  float2* Rpart = nullptr;       // ks2 x NP x NP
+  float2* kc = nullptr;          // N x N
+  int ks1 = 1, ks2 = 1;
+  CUtensorMap map_g1[4];         // Lks hi, lo; Rs hi, lo
+  CUtensorMap map_g2[4];         // Ls hi, lo; Rs hi, lo
+};
 struct GemmRunArgs {
   GemmInstance g;
+  bool split = false;
+  GemmSplit sp;
   cublasContext* blas = nullptr;
   bool fp64 = false;
   int Kdense = 0, D = 0, E = 0, nt = 0, obs_t0 = 0, store_every = 0, diag = 0;
@@ -122,6 +143,17 @@ struct GemmRunArgs {
 size_t gemm_partial_slots(int N);
 int gemm_setup(const GemmSetupArgs& a, cudaStream_t st);
 int gemm_propagate(const GemmRunArgs& a, cudaStream_t st);
+// FP32 pieces of the GEMM schedule reused by the split-precision one
+void gemm_init_split(const GemmInstance& g, const double2* rho0, cudaStream_t st);
+void gemm_obs_split(const GemmInstance& g, int E, double2* obs_out, cudaStream_t st);
+void gemm_drive_split(const GemmInstance& g, int D, const double* f, int nt, int step, cudaStream_t st);
+// split-precision schedule (lgb_gemm_tc.cu)
+int split_padded_dim(int N);
+size_t split_partial_slots(int N);
+size_t split_tpart_elems(int NP, int Kd, int n_sm, bool bf16);
+size_t split_rpart_elems(int NP, int Kd, int n_sm, bool bf16);
+int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_sm, cudaStream_t st);
+int split_propagate(const GemmRunArgs& a, cudaStream_t st);
 
 }  // namespace lgb
 
@@ -184,5 +216,6 @@ struct lgb_plan {
   // grid-wide GEMM schedule
   cublasContext* blas = nullptr;
   std::vector<lgb::GemmInstance> gemm;
+  std::vector<lgb::GemmSplit> gsplit;     // split-precision operands (3xTF32 / 3xBF16 GEMM schedule)
   double2* d_gtmp = nullptr;
 };

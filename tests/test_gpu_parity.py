@@ -19,6 +19,8 @@ pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
 TOL32 = 1e-5
+# 3xBF16 (reported path, not the chosen one): operands to ~2^-17 relative
+TOLBF = 1e-3
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -264,7 +266,8 @@ def _digest(*arrays):
     return h.hexdigest()
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32), ("3xtf32", TOL32),
+                                      ("3xbf16", TOLBF)])
 def test_gue256_golden(golden, prec, tol):
     g = golden("gue256")
     w = W.gue_instance(N=256, K=4, seed=2)
@@ -275,7 +278,8 @@ def test_gue256_golden(golden, prec, tol):
     assert np.abs(rho - g["rho"]).max() < tol
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32), ("3xtf32", TOL32),
+                                      ("3xbf16", TOLBF)])
 def test_gue1024_golden(golden, prec, tol):
     g = golden("gue1024")
     w = W.gue_instance(N=1024, K=8, scale=0.02, rank=4, seed=4, dt=0.005, nt=1000)
@@ -289,7 +293,8 @@ def test_gue1024_golden(golden, prec, tol):
     assert abs(np.trace(rho) - g["trace"]) < tol * 10
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32), ("3xtf32", TOL32),
+                                      ("3xbf16", TOLBF)])
 @pytest.mark.parametrize("kind", ["dense", "diag"])
 def test_gemm_schedule_vs_oracle(prec, tol, kind):
     rng = np.random.default_rng(31)
@@ -311,7 +316,8 @@ def test_gemm_schedule_vs_oracle(prec, tol, kind):
             assert np.abs(res["states"][b][k] - states[3 * k + 2]).max() < tol
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32)])
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32), ("3xtf32", TOL32),
+                                      ("3xbf16", TOLBF)])
 def test_gemm_schedule_driven_vs_oracle(prec, tol):
     rng = np.random.default_rng(32)
     dims = [12, 100]
