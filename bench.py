@@ -278,6 +278,8 @@ def run_gpu(args):
     line["clocks"] = ch["clocks"]
     if not args.no_adjoint:
         line["adjoint"] = measure_adjoint(args, dev)
+    if not args.no_large_n:
+        line["large_n"] = measure_large_n(args, dev)
     # CPU baseline (oracle port of the reference's dense algorithm) and accuracy
     if not args.no_cpu:
         line["cpu_baseline"], line["accuracy"] = cpu_baseline_and_accuracy(
@@ -330,6 +332,66 @@ def measure_adjoint(args, dev):
                 fwd_tflops=flops / (f / 1e3) / 1e12,
                 note="fwd: FP32 CTA kernel with checkpoints; bwd: recompute + costate kernel "
                      "(includes the gradient contractions); targets zero")
+
+
+# ---------------------------------------------------------------------------
+# single large instances (GEMM schedule): the split-precision tensor-core
+# GEMMs against the plain FP32 GEMMs
+# ---------------------------------------------------------------------------
+def measure_large_n(args, dev):
+    """GUE N=256 (K=4, dt=0.01) and N=1024 (K=8, scale 0.02, rank-4 rho0,
+    dt=0.005): ms per RK4 step of each path over ``--large-nt`` steps, and the
+    max-abs rho error after 10 steps against the FP64 GPU check path (itself
+    within 1e-12 of the reference's complex128 result on the fixtures)."""
+    import torch
+    from pyqed_gb300 import workloads as W
+    from pyqed_gb300.engine import Propagator, pack
+    out = {}
+    cases = [("gue256", dict(N=256, K=4, seed=2, dt=0.01, nt=10000)),
+             ("gue1024", dict(N=1024, K=8, scale=0.02, rank=4, seed=4, dt=0.005, nt=1000))]
+    for name, kw in cases:
+        w = W.gue_instance(**kw)
+        N, K, dt = kw["N"], kw["K"], kw["dt"]
+        H, C, R0 = pack([w["H"]]), pack(w["c_ops"]), pack([w["rho0"]])
+
+        def run(prec, nt, timed):
+            prop = Propagator([N], nt=nt, dt=dt, n_cops=K, cops_kind="dense", precision=prec,
+                              schedule="gemm", device=dev)
+            prop.set_operators(H, C)
+            r0 = prop.to_device(R0)
+            o = prop.alloc_outputs(want_obs=False, want_rho=True)
+            ms = None
+            if timed:
+                prop.propagate_device(r0, None, o)  # warm-up (library heuristics, caches)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                prop.propagate_device(r0, None, o)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / nt
+            else:
+                prop.propagate_device(r0, None, o)
+                torch.cuda.synchronize()
+            prop.check_errors()
+            rho = prop.unpack_rho(o[1])[0]
+            prop.close()
+            return ms, rho
+        _, ref = run("fp64", 10, False)
+        flops = 64 * (1 + K) * N ** 3
+        res = {}
+        for prec in ("3xtf32", "3xbf16", "fp32"):
+            ms, _ = run(prec, args.large_nt, True)
+            _, r10 = run(prec, 10, False)
+            res[prec] = dict(ms_per_step=ms, tflops_algorithmic=flops / (ms / 1e3) / 1e12,
+                             max_abs_err_rho_10_steps=float(np.abs(r10 - ref).max()))
+        for prec in ("3xtf32", "3xbf16"):
+            res[prec]["speedup_over_fp32"] = res["fp32"]["ms_per_step"] / res[prec]["ms_per_step"]
+        out[name] = dict(N=N, K=K, dt=dt, steps_timed=args.large_nt, paths=res,
+                         reference="FP64 GPU GEMM schedule, 10 steps")
+    out["note"] = ("split paths: hand-written TMA + tcgen05 complex GEMMs (lgb_gemm_tc.cu); "
+                   "fp32: cuBLAS CGEMM, pedantic math; algorithmic 64(1+K)N^3 flops per step")
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -460,9 +522,20 @@ def main():
                     help="time only the adjoint (fwd + bwd) on the driven workload")
     ap.add_argument("--adj-n-inst", type=int, default=256)
     ap.add_argument("--adj-nt", type=int, default=2000)
+    ap.add_argument("--no-large-n", action="store_true",
+                    help="skip the single large-instance (GEMM schedule) section")
+    ap.add_argument("--large-nt", type=int, default=100)
+    ap.add_argument("--only-large-n", action="store_true",
+                    help="run only the single large-instance (GEMM schedule) section")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.only_large_n:
+        import torch
+        from pyqed_gb300.build import build
+        build()
+        print(json.dumps(dict(large_n=measure_large_n(args, torch.device("cuda", 0)))))
         return
     if args.only_adjoint:
         import torch
