@@ -35,6 +35,7 @@
 // stops.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "lgb_common.cuh"
@@ -75,11 +76,13 @@ template <> struct Elem<true> {
   }
 };
 
+// Two thread groups (the warps of TMEM lane quarters 0-1 and 2-3) run separate
+// instances when NP <= 32; otherwise group 0 is the whole CTA.
 struct TcShared {
-  uint64_t mbar;
+  uint64_t mbar[2];
   uint32_t tmem_base;
-  int next;
-  float2 red[kMaxEops][kWarps];  // per-warp observable partials
+  int next[2];
+  float2 red[2][kMaxEops][kWarps];  // per-warp observable partials
 };
 
 // Shared-memory geometry of one instance.  All operands are K-major with
@@ -149,39 +152,71 @@ __device__ __forceinline__ uint64_t dadd(uint64_t d, uint32_t off) { return d + 
 
 // The 6 K-loops of one RK4 stage (single issuing thread), all at N = 2 NP
 // into one accumulator.
+// mshift: the M-side windows start this many bytes before the buffers, so
+// that the instance's rows land in TMEM lanes 64..127 (second instance of a
+// CTA that runs two).
 template <bool BF16, int NP>
-__device__ __forceinline__ void issue_stage(uint32_t d, uint32_t base) {
+__device__ __forceinline__ void issue_stage(uint32_t d, uint32_t base, uint32_t mshift) {
   using G = Geo<BF16, NP>;
   constexpr uint32_t id = idesc(Elem<BF16>::kFmt, 128, 2 * NP, false, false);
-  const uint64_t dA = sdesc(base + G::OFF_A, 128, G::SBO_S);
-  const uint64_t dXM = sdesc(base + G::OFF_XM, 128, G::SBO_S);
+  const uint64_t dAm = sdesc(base + G::OFF_A - mshift, 128, G::SBO_S);  // A as M side
+  const uint64_t dAn = sdesc(base + G::OFF_A, 128, G::SBO_S);           // A as N side
+  const uint64_t dXM = sdesc(base + G::OFF_XM - mshift, 128, G::SBO_S);
   const uint64_t dXT = sdesc(base + G::OFF_XT, G::LBO_T, G::SBO_T);
   // A X: A_hi X_hi, A_hi X_lo, A_lo X_hi
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dA, s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, s > 0 ? 1u : 0u);
+    mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, s > 0 ? 1u : 0u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dA, s * G::KSTEP_S), dadd(dXT, G::LVL_T + s * G::KSTEP_T), id, 1u);
+    mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, G::LVL_T + s * G::KSTEP_T), id, 1u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dA, G::LVL_S + s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, 1u);
+    mma<BF16>(d, dadd(dAm, G::LVL_S + s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, 1u);
   // X A^dag = (-i X) (i A^dag): X_hi A_hi, X_hi A_lo, X_lo A_hi
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dXM, s * G::KSTEP_S), dadd(dA, s * G::KSTEP_S), id, 1u);
+    mma<BF16>(d, dadd(dXM, s * G::KSTEP_S), dadd(dAn, s * G::KSTEP_S), id, 1u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dXM, s * G::KSTEP_S), dadd(dA, G::LVL_S + s * G::KSTEP_S), id, 1u);
+    mma<BF16>(d, dadd(dXM, s * G::KSTEP_S), dadd(dAn, G::LVL_S + s * G::KSTEP_S), id, 1u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dXM, G::LVL_S + s * G::KSTEP_S), dadd(dA, s * G::KSTEP_S), id, 1u);
+    mma<BF16>(d, dadd(dXM, G::LVL_S + s * G::KSTEP_S), dadd(dAn, s * G::KSTEP_S), id, 1u);
 }
 
-__device__ __forceinline__ void sync_for_mma() {
+// Barriers of a thread group: the whole CTA (GR = 1) or one half of it (GR = 2,
+// named barriers 1 and 2 of 256 threads).
+template <int GR>
+__device__ __forceinline__ void gsync(int g) {
+  if constexpr (GR == 1) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(kThreads / GR) : "memory");
+  }
+}
+template <int GR>
+__device__ __forceinline__ bool gor(int g, bool pred) {
+  if constexpr (GR == 1) {
+    return __syncthreads_or(pred) != 0;
+  } else {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 q, %1, 0;\n\t"
+        "bar.red.or.pred p, %2, %3, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "r"(g + 1), "r"(kThreads / GR)
+        : "memory");
+    return r != 0;
+  }
+}
+template <int GR>
+__device__ __forceinline__ void sync_for_mma(int g) {
   fence_async_smem();
   fence_before_sync();
-  __syncthreads();
+  gsync<GR>(g);
 }
 
 // Store 4 consecutive K elements of one operand row (16 bytes TF32, 8 bytes BF16).
@@ -203,19 +238,23 @@ __device__ __forceinline__ void st4(unsigned char* base, const float* v) {
 // q = w & 3 and owns columns [(w >> 2) NP/4, (w >> 2 + 1) NP/4) of its lane;
 // lane l of the warp is TMEM lane 32 q + l = M row (c, i) with c = l >> 4,
 // i = 16 q + (l & 15); its partner (1 - c, i) is lane l ^ 16.
-template <bool BF16, int NP>
+template <bool BF16, int NP, int GR>
 __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem, TcShared& sh,
-                            uint32_t& phase, bool& alive) {
+                            const int grp, uint32_t& phase, bool& alive) {
   using El = Elem<BF16>;
   using G = Geo<BF16, NP>;
   using ET = typename El::T;
-  constexpr int NPQ = NP / 4;  // columns per thread
-  constexpr int NG = NPQ / 4;  // groups of 4 columns
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, cg = warp >> 2;
-  const int c = lane >> 4;                   // 0: real part, 1: imaginary part
-  const int i = quarter * 16 + (lane & 15);  // row
+  constexpr int kT = kThreads / GR;  // threads of the group
+  constexpr int kW = kT / 32;        // warps of the group
+  constexpr int NPQ = NP / 4;        // columns per thread
+  constexpr int NG = NPQ / 4;        // groups of 4 columns
+  const int gwarp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int quarter = gwarp & 3, cg = gwarp >> 2;  // TMEM lane quarter, column group
+  // group-local warp and thread index (GR = 2: the group holds quarters 2 grp, 2 grp + 1)
+  const int warp = GR == 1 ? gwarp : (cg * 2 + (gwarp & 1));
+  const int tid = warp * 32 + lane;
+  const int c = lane >> 4;                              // 0: real part, 1: imaginary part
+  const int i = (GR == 1 ? quarter : (quarter & 1)) * 16 + (lane & 15);  // row
   const bool row_ok = i < NP;
   const int j0 = cg * NPQ;                   // first owned column
   const int N = p.dims[b];
@@ -233,12 +272,15 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const float2* Gt = reinterpret_cast<const float2*>(p.Gt) + (long long)p.n_drive * wo;
   const float2* Dm = reinterpret_cast<const float2*>(p.Dm) + wo;
   const float2* OtF = p.OtF + (long long)E * wo;
-  const uint32_t tlane = sh.tmem_base + ((uint32_t)(quarter * 32) << 16);
+  const uint32_t tmem_d = sh.tmem_base + (uint32_t)(grp * 64);
+  const uint32_t mshift = (uint32_t)grp * 8u * G::SBO_S;  // 64 rows
+  const uint32_t tlane = tmem_d + ((uint32_t)(quarter * 32) << 16);
+  uint64_t* mbar = &sh.mbar[grp];
 
   // ---- A buffer: rows (0, r) = Ar[r], (1, r) = Ai[r]; hi level then lo level.
   // Rebuilt every step when driven.
   auto build_a = [&](const float* f) {
-    for (int idx = tid; idx < NP * NP; idx += kThreads) {
+    for (int idx = tid; idx < NP * NP; idx += kT) {
       const int k = idx / NP, r = idx % NP;  // consecutive threads: consecutive rows
       float2 a = At0[k * NPS + r];           // A[r][k]
       if (f != nullptr) {
@@ -355,24 +397,27 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         fx += __shfl_xor_sync(0xffffffffu, fx, o);
         fy += __shfl_xor_sync(0xffffffffu, fy, o);
       }
-      if (lane == 0) sh.red[e][warp] = make_float2(fx, fy);
+      if (lane == 0) sh.red[grp][e][warp] = make_float2(fx, fy);
     }
     return fin;
   };
-  // Part 2 (its barrier follows part 1): warp e folds the kWarps partials of
-  // observable e and writes row ``row``; returns whether any element was not finite.
+  // Part 2 (its barrier follows part 1): warp w folds the per-warp partials of
+  // observables w, w + kW, .. and writes row ``row``; returns whether any
+  // element was not finite.
   auto obs_finish = [&](bool fin, int row) -> bool {
-    const bool anybad = __syncthreads_or(!fin) != 0;
-    if (warp < E && p.obs_out != nullptr) {
-      float2 v = lane < kWarps ? sh.red[warp][lane] : make_float2(0.f, 0.f);
+    const bool anybad = gor<GR>(grp, !fin);
+    if (p.obs_out != nullptr) {
+      for (int e = warp; e < E; e += kW) {
+        float2 v = lane < kW ? sh.red[grp][e][lane] : make_float2(0.f, 0.f);
 #pragma unroll
-      for (int o = kWarps / 2; o > 0; o >>= 1) {
-        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-      }
-      if (lane == 0) {
-        const long long nrows = (long long)p.nt + p.obs_t0;
-        p.obs_out[((long long)b * nrows + row) * E + warp] = make_double2((double)v.x, (double)v.y);
+        for (int o = kW / 2; o > 0; o >>= 1) {
+          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (lane == 0) {
+          const long long nrows = (long long)p.nt + p.obs_t0;
+          p.obs_out[((long long)b * nrows + row) * E + e] = make_double2((double)v.x, (double)v.y);
+        }
       }
     }
     return anybad;
@@ -380,11 +425,11 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
 
   // Bounded wait for the last commit; on time-out mark the instance and stop.
   auto wait_mma = [&]() -> bool {
-    const bool ok = mbar_wait(&sh.mbar, phase, kSpinLimit);
+    const bool ok = mbar_wait(mbar, phase, kSpinLimit);
     phase ^= 1u;
-    if (__syncthreads_or(!ok)) {
+    if (gor<GR>(grp, !ok)) {
       if (tid == 0) p.err[b] = 5;  // LGB_ERR_TIMEOUT
-      mbar_wait(&sh.mbar, phase ^ 1u, kSpinLimit);
+      mbar_wait(mbar, phase ^ 1u, kSpinLimit);
       alive = false;
       return false;
     }
@@ -425,8 +470,8 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       dc = dc || (d.y != 0.f);
     }
   }
-  const bool dgeneral = __syncthreads_or(off) != 0;
-  const bool dcomplex = __syncthreads_or(dc) != 0;
+  const bool dgeneral = gor<GR>(grp, off);
+  const bool dcomplex = gor<GR>(grp, dc);
   const bool dfast = diag && !dgeneral && !dcomplex;
   const int dpos = (i >= j0 && i < j0 + NPQ) ? i - j0 : -1;
   const float dd = (dfast && dpos >= 0 && i < N) ? Dm[i * NPS + i].x : 0.f;
@@ -460,11 +505,11 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     }
 #pragma unroll 1
     for (int stage = 0; stage < 4; ++stage) {
-      sync_for_mma();
+      sync_for_mma<GR>(grp);
       if (tid == 0) {
         fence_after_sync();
-        issue_stage<BF16, NP>(sh.tmem_base, sbase);
-        mma_commit(&sh.mbar);
+        issue_stage<BF16, NP>(tmem_d, sbase, mshift);
+        mma_commit(mbar);
       }
       if (stage == 0 && pend_row >= 0) pend_fin = obs_partials();
       if (!wait_mma()) break;
@@ -588,7 +633,13 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   }
   // TMEM reads of this instance are done before the next instance's first MMA
   fence_before_sync();
-  __syncthreads();
+  gsync<GR>(grp);
+}
+
+// Shared memory of one group in two-instance mode (NP <= 32), 1 KB aligned.
+template <bool BF16>
+__host__ __device__ constexpr uint32_t dual_bytes() {
+  return (Geo<BF16, 32>::BYTES + 1023u) / 1024u * 1024u;
 }
 
 template <bool BF16>
@@ -598,7 +649,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
   __shared__ TcShared sh;
   const int tid = threadIdx.x;
   if (tid == 0) {
-    mbar_init(&sh.mbar, 1);
+    mbar_init(&sh.mbar[0], 1);
+    mbar_init(&sh.mbar[1], 1);
     mbar_fence_init();
   }
   if (tid < 32) {
@@ -610,18 +662,51 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
   fence_after_sync();
   uint32_t phase = 0;
   bool alive = true;
+  int small = -1;
+  // Instances with NP >= 48 (the queue is sorted by size): the whole CTA.
   while (alive) {
-    if (tid == 0) sh.next = atomicAdd(queue, 1);
+    if (tid == 0) sh.next[0] = atomicAdd(queue, 1);
     __syncthreads();
-    const int item = sh.next;
+    const int item = sh.next[0];
     __syncthreads();
     if (item >= n_items) break;
     const int b = order[item];
-    switch (p.npad[b]) {
-      case 16: tc_instance<BF16, 16>(p, b, smem, sh, phase, alive); break;
-      case 32: tc_instance<BF16, 32>(p, b, smem, sh, phase, alive); break;
-      case 48: tc_instance<BF16, 48>(p, b, smem, sh, phase, alive); break;
-      default: tc_instance<BF16, 64>(p, b, smem, sh, phase, alive); break;
+    if (p.npad[b] <= 32) {
+      small = item;
+      break;
+    }
+    if (p.npad[b] == 48) {
+      tc_instance<BF16, 48, 1>(p, b, smem, sh, 0, phase, alive);
+    } else {
+      tc_instance<BF16, 64, 1>(p, b, smem, sh, 0, phase, alive);
+    }
+  }
+  // NP <= 32: the warps of TMEM lane quarters 0-1 and those of quarters 2-3
+  // each run their own instances (own shared memory, TMEM columns, mbarrier
+  // and named barrier; the second group's M-side operand windows start 64
+  // rows early so that its rows land in lanes 64..127), so that one group's
+  // MMAs overlap the other's epilogue.
+  if (alive && small >= 0) {
+    const int g = (tid >> 5 & 3) >> 1;  // TMEM lane quarters 0-1 or 2-3
+    unsigned char* sg = smem + g * dual_bytes<BF16>();
+    uint32_t ph = g == 0 ? phase : 0u;
+    int item = g == 0 ? small : -1;
+    bool galive = true;
+    while (galive) {
+      if (item < 0) {
+        if ((tid & 0x1bf) == 0) sh.next[g] = atomicAdd(queue, 1);  // warp 0 / 2, lane 0
+        gsync<2>(g);
+        item = sh.next[g];
+        gsync<2>(g);
+      }
+      if (item >= n_items) break;
+      const int b = order[item];
+      if (p.npad[b] == 16) {
+        tc_instance<BF16, 16, 2>(p, b, sg, sh, g, ph, galive);
+      } else {
+        tc_instance<BF16, 32, 2>(p, b, sg, sh, g, ph, galive);
+      }
+      item = -1;
     }
   }
   fence_before_sync();
@@ -635,11 +720,13 @@ int tc_max_dim() { return 64; }
 
 int tc_smem_bytes(int precision, int npad) {
   const bool bf16 = precision == LGB_PREC_BF16X3;
+  // instances of at most npad: one at a time for NP >= 48, two for NP <= 32
+  const int dual = bf16 ? 2 * (int)dual_bytes<true>() : 2 * (int)dual_bytes<false>();
   switch (npad) {
-    case 16: return bf16 ? (int)Geo<true, 16>::BYTES : (int)Geo<false, 16>::BYTES;
-    case 32: return bf16 ? (int)Geo<true, 32>::BYTES : (int)Geo<false, 32>::BYTES;
-    case 48: return bf16 ? (int)Geo<true, 48>::BYTES : (int)Geo<false, 48>::BYTES;
-    default: return bf16 ? (int)Geo<true, 64>::BYTES : (int)Geo<false, 64>::BYTES;
+    case 16:
+    case 32: return dual;
+    case 48: return std::max(dual, bf16 ? (int)Geo<true, 48>::BYTES : (int)Geo<false, 48>::BYTES);
+    default: return std::max(dual, bf16 ? (int)Geo<true, 64>::BYTES : (int)Geo<false, 64>::BYTES);
   }
 }
 
