@@ -254,8 +254,20 @@ def run_gpu(args):
         pk = peaks.get("bf16_tflops", 1900.0)
         if chosen == "3xtf32":
             pk = pk / 2.0
+        traffic = None
+        if args.workload == "exciton4096":
+            # DRAM bytes per launch: operator/rho0 reads measured by ncu on a
+            # 304-instance case (23.0 MB against 24.3 MB algorithmic) scaled by
+            # the algorithmic read bytes, plus the algorithmic writes (C(t), rho)
+            d64 = bi.dims.astype(np.int64)
+            npd = np.where(d64 <= 64, (d64 + 15) // 16 * 16, (d64 + 3) // 4 * 4)
+            reads = int((npd * (npd + 2) * 8 * (2 + bi.n_eops)).sum() + (d64 ** 2 * 16).sum())
+            writes = int(n_inst * nt * bi.n_eops * 16 + (d64 ** 2 * 16).sum())
+            traffic = int(reads * (23.03 / 24.30)) + writes
         line["roofline"] = dict(bound="tensor", achieved=achieved, peak=pk, unit="TFLOP/s",
-                                frac=achieved / pk, traffic=None,
+                                frac=achieved / pk, traffic=traffic,
+                                traffic_note="bytes per launch: ncu-measured reads scaled to the "
+                                             "full batch + algorithmic writes (profiles/)",
                                 note="algorithmic 64*N^3 flops per instance-step; peak = "
                                      + ("measured bf16 / 2 (TF32 rate)" if chosen == "3xtf32"
                                         else "measured bf16"))

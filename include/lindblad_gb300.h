@@ -175,6 +175,22 @@ typedef struct {
 
 int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
 
+/* Tuning options of a plan; no counterpart in the reference.  They change
+ * how the work is scheduled, never the arithmetic's result beyond rounding
+ * order, and stay in force until changed.  pyqed_gb300.autotune picks them
+ * by timing candidates.
+ *   LGB_OPT_TC_PAIRS   tensor-core kernel: 1 (default) runs two instances per
+ *                      CTA when NP <= 32, 0 one at a time
+ *   LGB_OPT_GEMM_WAVES split-precision GEMM schedule: the split-K factors fill
+ *                      1 (default) or 2 waves of CTAs on the SMs
+ * Returns LGB_ERR_INVALID_ARG for an unknown option or value. */
+typedef enum {
+  LGB_OPT_TC_PAIRS = 1,
+  LGB_OPT_GEMM_WAVES = 2
+} lgb_option_t;
+
+int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value);
+
 /* ---- propagation without device allocation ---------------------------------
  * No counterpart in the reference: pyqed is pure Python and never manages
  * device memory.

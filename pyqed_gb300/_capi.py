@@ -39,8 +39,10 @@ SCHED_NAME = {v: k for k, v in SCHED.items()}
 EXPORTS = [
     "lgb_get_version", "lgb_status_string", "lgb_plan_create", "lgb_plan_destroy",
     "lgb_plan_set_operators", "lgb_plan_propagate", "lgb_plan_errors", "lgb_plan_get_info",
-    "lgb_propagate_noalloc", "lgb_plan_adjoint",
+    "lgb_propagate_noalloc", "lgb_plan_adjoint", "lgb_plan_set_option",
 ]
+# tuning options (lgb_option_t)
+OPT = {"tc_pairs": 1, "gemm_waves": 2}
 FLAG_ADJOINT = 1
 
 
@@ -109,6 +111,8 @@ def lib():
     L.lgb_plan_errors.argtypes = [vp, ctypes.POINTER(i32)]
     L.lgb_plan_get_info.restype = ctypes.c_int
     L.lgb_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+    L.lgb_plan_set_option.restype = ctypes.c_int
+    L.lgb_plan_set_option.argtypes = [vp, i32, i32]
     L.lgb_plan_adjoint.restype = ctypes.c_int
     L.lgb_plan_adjoint.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, vp]
     L.lgb_propagate_noalloc.restype = ctypes.c_int

@@ -84,17 +84,27 @@ def propagate_batch(H, c_ops, rho0, dt, Nt, e_ops=None, *, obs_t0=True, store_ev
                     precision="fp32", schedule="auto", drive_ops=None, drive=None,
                     device=None, return_rho=True):
     """Propagate a batch; returns dict(observables (n, rows, E), rho list,
-    states list, info)."""
+    states list, info).  ``schedule``: "auto", "cta", "gemm" or "tune" (the
+    autotuner times the candidates first, see ``pyqed_gb300.autotune``)."""
     bi = prepare_batch(H, c_ops, rho0, e_ops, drive_ops)
     drive_shared = True
     if bi.n_drive:
         drive = np.asarray(drive, dtype=np.float64)
         drive_shared = drive.ndim == 2
+    options = {}
+    tuned = None
+    if schedule == "tune":
+        from .autotune import tune
+        tuned = tune(bi, dt=dt, precision=precision, obs_t0=obs_t0, drive=drive,
+                     drive_shared=drive_shared, device=device)
+        schedule, options = tuned["schedule"], tuned["options"]
     prop = Propagator(bi.dims, nt=Nt, dt=dt, n_cops=bi.n_cops, cops_kind=bi.cops_kind,
                       n_eops=bi.n_eops, n_drive=bi.n_drive, obs_t0=obs_t0,
                       store_every=store_every, precision=precision, schedule=schedule,
                       drive_shared=drive_shared, device=device)
     try:
+        for k, v in options.items():
+            prop.set_option(k, v)
         prop.set_operators(bi.H, bi.cops, bi.eops, bi.dops)
         d = torch.from_numpy(drive.ravel()).to(prop.device) if bi.n_drive else None
         out = prop.alloc_outputs(want_obs=True, want_rho=return_rho,
@@ -102,6 +112,8 @@ def propagate_batch(H, c_ops, rho0, dt, Nt, e_ops=None, *, obs_t0=True, store_ev
         obs, rho, st = prop.propagate_device(prop.to_device(bi.rho0), d, out)
         prop.check_errors()
         res = dict(info=prop.info())
+        if tuned is not None:
+            res["tuned"] = tuned
         res["observables"] = (prop.unpack_obs(obs) if obs is not None
                               else np.zeros((prop.n_inst, Nt + int(obs_t0), 0), complex))
         res["rho"] = prop.unpack_rho(rho) if rho is not None else None

@@ -41,6 +41,8 @@ int upload(lgb_plan* pl, T** dptr, const std::vector<T>& v) {
 
 void free_plan(lgb_plan* pl) {
   if (pl->blas) cublasDestroy(pl->blas);
+  if (pl->cap_stream) cudaStreamDestroy(pl->cap_stream);
+  pl->cap_stream = nullptr;
   pl->blas = nullptr;
   for (void* p : pl->allocations) cudaFree(p);
   pl->allocations.clear();
@@ -328,8 +330,8 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
           s = s ? s : dalloc(pl, &q.Rs[l], (size_t)2 * q.NP * q.Wp * ses);
           s = s ? s : dalloc(pl, &q.Lks[l], (size_t)Kd * 2 * q.NP * q.NP * ses);
         }
-        s = s ? s : dalloc(pl, &q.Tpart, Kd ? lgb::split_tpart_elems(q.NP, Kd, pl->n_sm, bf16) * sizeof(float2) : 0);
-        s = s ? s : dalloc(pl, &q.Rpart, lgb::split_rpart_elems(q.NP, Kd, pl->n_sm, bf16) * sizeof(float2));
+        s = s ? s : dalloc(pl, &q.Tpart, Kd ? lgb::split_tpart_elems(q.NP, Kd, 2 * pl->n_sm, bf16) * sizeof(float2) : 0);
+        s = s ? s : dalloc(pl, &q.Rpart, lgb::split_rpart_elems(q.NP, Kd, 2 * pl->n_sm, bf16) * sizeof(float2));
         s = s ? s : dalloc(pl, &q.kc, (size_t)pl->dims[b] * pl->dims[b] * sizeof(float2));
       }
     }
@@ -341,6 +343,17 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
         // plain library GEMMs: no reduced-precision tensor-op substitutions
         cublasSetMathMode(pl->blas, CUBLAS_PEDANTIC_MATH);
       }
+    }
+    // step counter, a private capture stream and a fixed cuBLAS workspace, so
+    // that blocks of RK4 steps can be captured into CUDA graphs
+    constexpr size_t kBlasWs = 32u << 20;
+    s = s ? s : dalloc(pl, &pl->d_ctr, sizeof(int));
+    s = s ? s : dalloc(pl, &pl->blas_ws, kBlasWs);
+    if (s == LGB_OK && cublasSetWorkspace(pl->blas, pl->blas_ws, kBlasWs) != CUBLAS_STATUS_SUCCESS)
+      s = LGB_ERR_CUDA;
+    if (s == LGB_OK && cudaStreamCreateWithFlags(&pl->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      pl->cap_stream = nullptr;
+      s = LGB_ERR_CUDA;
     }
   }
   if (s != LGB_OK) {
@@ -416,7 +429,7 @@ int lgb_plan_set_operators(lgb_plan_t plan, const double* H, const double* cops,
       s = lgb::gemm_setup(a, st);
       if (s == LGB_OK && !plan->gsplit.empty())
         s = lgb::split_setup(plan->gsplit[b], plan->gemm[b], pr.cops_kind == LGB_COPS_DENSE ? K : 0,
-                             pr.precision == LGB_PREC_BF16X3, plan->n_sm, st);
+                             pr.precision == LGB_PREC_BF16X3, plan->n_sm * plan->opt_waves, st);
     }
   } else {
     s = cuda_status(lgb::launch_setup(sp, pr.precision == LGB_PREC_FP64 ? 0 : 1, st));
@@ -434,6 +447,7 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   plan->last_stream = st;
   CtaParams p{};
+  p.tc_pairs = plan->opt_pairs;
   p.n_inst = pr.n_inst;
   p.n_cops = pr.n_cops;
   p.cops_kind = pr.cops_kind;
@@ -482,6 +496,8 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
       a.fp64 = pr.precision == LGB_PREC_FP64;
       a.split = !plan->gsplit.empty();
       if (a.split) a.sp = plan->gsplit[b];
+      a.ctr = plan->d_ctr;
+      a.cap = plan->cap_stream;
       a.Kdense = pr.cops_kind == LGB_COPS_DENSE ? pr.n_cops : 0;
       a.D = pr.n_drive;
       a.E = pr.n_eops;
@@ -649,6 +665,25 @@ int lgb_plan_errors(lgb_plan_t plan, int32_t* flags_host) {
   return LGB_OK;
 }
 
+int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value) {
+  if (plan == nullptr) return LGB_ERR_INVALID_ARG;
+  switch (option) {
+    case LGB_OPT_TC_PAIRS:
+      if (value != 0 && value != 1) return LGB_ERR_INVALID_ARG;
+      plan->opt_pairs = value;
+      return LGB_OK;
+    case LGB_OPT_GEMM_WAVES: {
+      if (value != 1 && value != 2) return LGB_ERR_INVALID_ARG;
+      plan->opt_waves = value;
+      const int Kd = plan->prob.cops_kind == LGB_COPS_DENSE ? plan->prob.n_cops : 0;
+      for (auto& q : plan->gsplit) lgb::split_set_ksplit(q, Kd, plan->n_sm * value);
+      return LGB_OK;
+    }
+    default:
+      return LGB_ERR_INVALID_ARG;
+  }
+}
+
 int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
   if (plan == nullptr || info == nullptr) return LGB_ERR_INVALID_ARG;
   info->schedule = plan->schedule;
@@ -666,7 +701,8 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
     const int per_stage = (dense ? (split ? 2 : 1) : 0) + 2;
     const int per_drive = pr.n_drive > 0 ? (split ? 3 : 1) : 0;
     const int init = 1 + (split ? 2 : 0) + (pr.obs_t0 && pr.n_eops ? 1 : 0);
-    info->launches_per_propagate = pr.n_inst * (init + pr.nt * (4 * per_stage + per_drive));
+    // (+1 per step: the step-counter increment; steps run as CUDA-graph replays when nt >= 32)
+    info->launches_per_propagate = pr.n_inst * (init + pr.nt * (4 * per_stage + per_drive + 1));
   }
   info->workspace_bytes = (int64_t)plan->ws_bytes;
   info->flops_per_step = plan->flops_per_step;

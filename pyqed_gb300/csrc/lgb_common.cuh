@@ -86,6 +86,7 @@ struct CtaParams {
   long long state_stride;    // complex elements between stored states (0: N*N)
   void* ystore;              // optional: every stage input, 4 * ycap x NP x NPS per instance
   int ycap;                  // steps held per instance in ystore
+  int tc_pairs;              // tensor-core kernel: two instances per CTA for NP <= 32
 };
 
 }  // namespace lgb

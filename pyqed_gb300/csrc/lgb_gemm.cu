@@ -142,7 +142,8 @@ __global__ void gemm_setup_kernel(GemmInstance g, const double2* H, const double
 // Driven instances: A(t) = A0 + sum_d f_d (i H_d) into Lbuf block 0 and its
 // adjoint into Rbuf block 1.
 template <typename T>
-__global__ void gemm_drive_kernel(GemmInstance g, int D, const double* f, int nt, int step) {
+__global__ void gemm_drive_kernel(GemmInstance g, int D, const double* f, int nt, const int* ctr) {
+  const int step = *ctr;
   using T2 = typename Cplx<T>::type;
   const int N = g.N;
   const long long NN = (long long)N * N;
@@ -251,13 +252,16 @@ __global__ void gemm_obs_kernel(GemmInstance g, int E, double2* obs_out, long lo
 // observables, checks finiteness and stores the state when asked.
 template <typename T>
 __global__ void __launch_bounds__(kEpiThreads) gemm_epilogue_kernel(
-    GemmInstance g, int stage, double dt, int diag, int E, double2* obs_out, long long row_index,
-    double2* state_out, double2* rho_out) {
+    GemmInstance g, int stage, double dt, int diag, int E, double2* obs_out, StepOut so) {
   using T2 = typename Cplx<T>::type;
   __shared__ double sbuf[kEpiThreads / 32];
   __shared__ double2 blk[16];
   const int N = g.N;
   const long long NN = (long long)N * N;
+  const int step = *so.ctr;
+  const long long row_index = (long long)step + so.obs_t0;
+  double2* state_out = (stage == 3) ? so.state_at(step, NN) : nullptr;
+  double2* rho_out = (stage == 3 && step == so.nt - 1) ? so.rho_out : nullptr;
   const T cst = (T)((stage == 2) ? dt : 0.5 * dt);
   const T sixth = (T)(dt / 6.0);
   double ox[16], oy[16];
@@ -315,6 +319,8 @@ __global__ void __launch_bounds__(kEpiThreads) gemm_epilogue_kernel(
   }
 }
 
+__global__ void step_inc_kernel(int* ctr) { *ctr += 1; }
+
 int epi_grid(int N) {
   const long long NN = (long long)N * N;
   long long b = (NN + (long long)kEpiThreads * kEpiElems - 1) / ((long long)kEpiThreads * kEpiElems);
@@ -358,20 +364,26 @@ static int gemm_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
   GemmInstance g = a.g;
   const int N = g.N, K = a.Kdense, W = g.W;
   const long long NN = (long long)N * N;
-  cublasSetStream(a.blas, st);
   const int grid = (int)std::min<long long>((NN + 255) / 256, 4096);
   const int egrid = epi_grid(N);
   const size_t esz = sizeof(typename Cplx<T>::type);
+  cublasSetStream(a.blas, st);
   gemm_init_kernel<T><<<grid, 256, 0, st>>>(g, a.rho0);
   if (a.obs_t0 && a.E > 0) gemm_obs_kernel<T><<<egrid, kEpiThreads, 0, st>>>(g, a.E, a.obs_out, 0);
+  if (cudaMemsetAsync(a.ctr, 0, sizeof(int), st) != cudaSuccess) return LGB_ERR_CUDA;
   if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
   using B_ = Blas<T>;
-  const typename B_::C one = B_::one(), zero = B_::zero();
-  for (int step = 0; step < a.nt; ++step) {
-    if (a.D > 0) gemm_drive_kernel<T><<<grid, 256, 0, st>>>(g, a.D, a.drive, a.nt, step);
-    const bool store = a.store_every > 0 && a.states_out != nullptr && ((step + 1) % a.store_every) == 0;
-    double2* sout = store ? a.states_out + ((step + 1) / a.store_every - 1) * NN : nullptr;
-    double2* rout = (step == a.nt - 1) ? a.rho_out : nullptr;
+  StepOut so;
+  so.ctr = a.ctr;
+  so.obs_t0 = a.obs_t0;
+  so.nt = a.nt;
+  so.store_every = a.store_every;
+  so.states_out = a.states_out;
+  so.rho_out = a.rho_out;
+  auto one_step = [&](cudaStream_t s) -> int {
+    const typename B_::C one = B_::one(), zero = B_::zero();
+    cublasSetStream(a.blas, s);
+    if (a.D > 0) gemm_drive_kernel<T><<<grid, 256, 0, s>>>(g, a.D, a.drive, a.nt, a.ctr);
     for (int stage = 0; stage < 4; ++stage) {
       if (K > 0) {
         // T_k = L_k X -> Lbuf blocks 2..K+1 (row-major, ld W); X = Rbuf rows 0..N-1
@@ -384,11 +396,14 @@ static int gemm_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
       // R = Lbuf (N x W) . Rbuf (W x N)
       if (gemm_rm<T>(a.blas, N, N, W, g.Lbuf, W, g.Rbuf, N, g.Rout, N) != CUBLAS_STATUS_SUCCESS)
         return LGB_ERR_CUDA;
-      gemm_epilogue_kernel<T><<<egrid, kEpiThreads, 0, st>>>(
-          g, stage, a.dt, a.diag, a.E, a.obs_out, (long long)step + a.obs_t0,
-          stage == 3 ? sout : nullptr, stage == 3 ? rout : nullptr);
+      gemm_epilogue_kernel<T><<<egrid, kEpiThreads, 0, s>>>(g, stage, a.dt, a.diag, a.E, a.obs_out, so);
     }
-  }
+    step_inc_kernel<<<1, 1, 0, s>>>(a.ctr);
+    return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+  };
+  const int r = run_steps(a.nt, st, a.cap, one_step);
+  cublasSetStream(a.blas, st);
+  if (r != LGB_OK) return r;
   if (a.nt == 0 && a.rho_out != nullptr)
     cudaMemcpyAsync(a.rho_out, a.rho0, NN * sizeof(double2), cudaMemcpyDeviceToDevice, st);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
@@ -406,9 +421,10 @@ void gemm_init_split(const GemmInstance& g, const double2* rho0, cudaStream_t st
 void gemm_obs_split(const GemmInstance& g, int E, double2* obs_out, cudaStream_t st) {
   gemm_obs_kernel<float><<<epi_grid(g.N), kEpiThreads, 0, st>>>(g, E, obs_out, 0);
 }
-void gemm_drive_split(const GemmInstance& g, int D, const double* f, int nt, int step, cudaStream_t st) {
+void gemm_drive_split(const GemmInstance& g, int D, const double* f, int nt, const int* ctr, cudaStream_t st) {
   const long long NN = (long long)g.N * g.N;
-  gemm_drive_kernel<float><<<(int)std::min<long long>((NN + 255) / 256, 4096), 256, 0, st>>>(g, D, f, nt, step);
+  gemm_drive_kernel<float><<<(int)std::min<long long>((NN + 255) / 256, 4096), 256, 0, st>>>(g, D, f, nt, ctr);
 }
+void gemm_step_inc(int* ctr, cudaStream_t st) { step_inc_kernel<<<1, 1, 0, st>>>(ctr); }
 
 }  // namespace lgb

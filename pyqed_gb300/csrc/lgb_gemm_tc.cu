@@ -368,8 +368,7 @@ __device__ void finish_obs_split(const GemmInstance& g, const double2* blk, int 
 template <bool BF16>
 __global__ void __launch_bounds__(256) split_epilogue_kernel(GemmInstance g, GemmSplit sp, int stage,
                                                              double dt, int diag, int E,
-                                                             double2* obs_out, long long row,
-                                                             double2* state_out, double2* rho_out) {
+                                                             double2* obs_out, StepOut so) {
   using T = typename SElem<BF16>::T;
   __shared__ float2 xt[32][33];
   __shared__ double red[8][16][2];
@@ -377,6 +376,10 @@ __global__ void __launch_bounds__(256) split_epilogue_kernel(GemmInstance g, Gem
   const int N = g.N, NP = sp.NP;
   const int tiles = (N + 31) / 32;
   const int i0 = (blockIdx.x / tiles) * 32, j0 = (blockIdx.x % tiles) * 32;
+  const int step = *so.ctr;
+  const long long row = (long long)step + so.obs_t0;
+  double2* state_out = stage == 3 ? so.state_at(step, (long long)N * N) : nullptr;
+  double2* rho_out = (stage == 3 && step == so.nt - 1) ? so.rho_out : nullptr;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const float cst = (float)((stage == 2) ? dt : 0.5 * dt);
   const float sixth = (float)(dt / 6.0);
@@ -537,12 +540,11 @@ int choose_ksplit(int tiles, int kblocks, int n_sm) {
   return best;
 }
 
+// (the kernel's shared-memory attribute is set once in split_setup, outside
+// any stream capture)
 template <bool BF16>
 cudaError_t launch_cgemm(const CUtensorMap* maps, const CgArgs& a, int ntile_n, int ntile_m, int nz,
                          cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(cgemm3_kernel<BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kGemmSmem);
-  if (e != cudaSuccess) return e;
   cgemm3_kernel<BF16><<<dim3(ntile_n, ntile_m, nz), kGThreads, kGemmSmem, st>>>(maps[0], maps[1], maps[2],
                                                                                maps[3], a);
   return cudaGetLastError();
@@ -566,6 +568,7 @@ int split_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
   split_trans_kernel<BF16><<<dim3(tiles, tiles), dim3(32, 8), 0, st>>>(
       reinterpret_cast<const float2*>(g.Rbuf), N, N, N, sp.Rs[0], sp.Rs[1], sp.Wp, 0);
   if (a.obs_t0 && a.E > 0) gemm_obs_split(g, a.E, a.obs_out, st);
+  if (cudaMemsetAsync(a.ctr, 0, sizeof(int), st) != cudaSuccess) return LGB_ERR_CUDA;
   if ((e = cudaGetLastError()) != cudaSuccess) return LGB_ERR_CUDA;
   // G1: T_k = L_k X, batched over k; G2: R = Ls . Rs^T
   CgArgs g1, g2;
@@ -585,39 +588,45 @@ int split_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
   g2.q_row0 = 0;
   g2.k0 = 0;
   g2.ksplit = sp.ks2;
-  g2.klen = sp.Wp / sp.ks2;
+  g2.klen = (int)(sp.Wp / sp.ks2);
   g2.out = sp.Rpart;
   g2.out_ld = NP;
   g2.out_split = (long long)NP * NP;
   g2.err = g.err;
   if (g1.klen % KT || g2.klen % KT) return LGB_ERR_INVALID_ARG;
-  for (int step = 0; step < a.nt; ++step) {
+  StepOut so;
+  so.ctr = a.ctr;
+  so.obs_t0 = a.obs_t0;
+  so.nt = a.nt;
+  so.store_every = a.store_every;
+  so.states_out = a.states_out;
+  so.rho_out = a.rho_out;
+  auto one_step = [&](cudaStream_t s) -> int {
     if (a.D > 0) {
-      gemm_drive_split(g, a.D, a.drive, a.nt, step, st);
+      gemm_drive_split(g, a.D, a.drive, a.nt, a.ctr, s);
       // A -> M-side block 0 (rows); A^dag -> N-side block 1 (transposed)
-      split_rows_kernel<BF16><<<dim3(grid, 1), 256, 0, st>>>(reinterpret_cast<const float2*>(g.Lbuf), g.W,
-                                                             0, N, N, sp.Ls[0], sp.Ls[1], sp.Wp, 0, 0);
-      split_trans_kernel<BF16><<<dim3(tiles, tiles), dim3(32, 8), 0, st>>>(
+      split_rows_kernel<BF16><<<dim3(grid, 1), 256, 0, s>>>(reinterpret_cast<const float2*>(g.Lbuf), g.W,
+                                                            0, N, N, sp.Ls[0], sp.Ls[1], sp.Wp, 0, 0);
+      split_trans_kernel<BF16><<<dim3(tiles, tiles), dim3(32, 8), 0, s>>>(
           reinterpret_cast<const float2*>(g.Rbuf) + NN, N, N, N, sp.Rs[0], sp.Rs[1], sp.Wp, NP);
     }
-    const bool store = a.store_every > 0 && a.states_out != nullptr && ((step + 1) % a.store_every) == 0;
-    double2* sout = store ? a.states_out + ((step + 1) / a.store_every - 1) * NN : nullptr;
-    double2* rout = (step == a.nt - 1) ? a.rho_out : nullptr;
     for (int stage = 0; stage < 4; ++stage) {
       if (K > 0) {
-        if ((e = launch_cgemm<BF16>(sp.map_g1, g1, NP / 128, NP / 64, K * sp.ks1, st)) != cudaSuccess)
+        if (launch_cgemm<BF16>(sp.map_g1, g1, NP / 128, NP / 64, K * sp.ks1, s) != cudaSuccess)
           return LGB_ERR_CUDA;
-        tsum_split_kernel<BF16><<<(int)std::min<long long>((K * NN + 255) / 256, 8192), 256, 0, st>>>(
+        tsum_split_kernel<BF16><<<(int)std::min<long long>((K * NN + 255) / 256, 8192), 256, 0, s>>>(
             sp.Tpart, sp.ks1, (long long)K * NP * NP, K, N, NP, sp.Ls[0], sp.Ls[1], sp.Wp);
       }
-      if ((e = launch_cgemm<BF16>(sp.map_g2, g2, NP / 128, NP / 64, sp.ks2, st)) != cudaSuccess)
+      if (launch_cgemm<BF16>(sp.map_g2, g2, NP / 128, NP / 64, sp.ks2, s) != cudaSuccess)
         return LGB_ERR_CUDA;
-      split_epilogue_kernel<BF16><<<tiles * tiles, dim3(32, 8), 0, st>>>(
-          g, sp, stage, a.dt, a.diag, a.E, a.obs_out, (long long)step + a.obs_t0,
-          stage == 3 ? sout : nullptr, stage == 3 ? rout : nullptr);
-      if ((e = cudaGetLastError()) != cudaSuccess) return LGB_ERR_CUDA;
+      split_epilogue_kernel<BF16><<<tiles * tiles, dim3(32, 8), 0, s>>>(g, sp, stage, a.dt, a.diag, a.E,
+                                                                        a.obs_out, so);
     }
-  }
+    gemm_step_inc(a.ctr, s);
+    return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+  };
+  const int r = run_steps(a.nt, st, a.cap, one_step);
+  if (r != LGB_OK) return r;
   if (a.nt == 0 && a.rho_out != nullptr)
     cudaMemcpyAsync(a.rho_out, a.rho0, NN * sizeof(double2), cudaMemcpyDeviceToDevice, st);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
@@ -684,12 +693,19 @@ int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_s
          make_map(&sp.map_g1[2], sp.Rs[0], bf16, 2LL * NP, sp.Wp, kQRows) &&
          make_map(&sp.map_g1[3], sp.Rs[1], bf16, 2LL * NP, sp.Wp, kQRows);
   if (!ok) return LGB_ERR_UNSUPPORTED;
-  // split-K factors
-  const int KT = kRowBytes / (bf16 ? 2 : 4);
-  const int t2 = (NP / 128) * (NP / 64);
-  sp.ks2 = choose_ksplit(t2, sp.Wp / KT, n_sm);
-  sp.ks1 = Kd > 0 ? choose_ksplit(t2 * Kd, NP / KT, n_sm) : 1;
-  return LGB_OK;
+  split_set_ksplit(sp, Kd, n_sm);
+  const cudaError_t e = bf16 ? cudaFuncSetAttribute(cgemm3_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)kGemmSmem)
+                             : cudaFuncSetAttribute(cgemm3_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)kGemmSmem);
+  return e == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
+void split_set_ksplit(GemmSplit& sp, int Kd, int cta_budget) {
+  const int KT = kRowBytes / (sp.bf16 ? 2 : 4);
+  const int t2 = (sp.NP / 128) * (sp.NP / 64);
+  sp.ks2 = choose_ksplit(t2, (int)(sp.Wp / KT), cta_budget);
+  sp.ks1 = Kd > 0 ? choose_ksplit(t2 * Kd, sp.NP / KT, cta_budget) : 1;
 }
 
 size_t split_tpart_elems(int NP, int Kd, int n_sm, bool bf16) {

@@ -95,6 +95,18 @@ struct GemmInstance {
   int* counter = nullptr;        // last-block ticket
   int* err = nullptr;            // instance status
 };
+// Step-dependent outputs of the stage-3 epilogue, resolved on the device from
+// the step counter (so that a captured step can be replayed).
+struct StepOut {
+  const int* ctr = nullptr;
+  int obs_t0 = 0, nt = 0, store_every = 0;
+  double2* states_out = nullptr;
+  double2* rho_out = nullptr;
+  __host__ __device__ double2* state_at(int step, long long NN) const {
+    if (store_every <= 0 || states_out == nullptr || (step + 1) % store_every != 0) return nullptr;
+    return states_out + (long long)((step + 1) / store_every - 1) * NN;
+  }
+};
 struct GemmSetupArgs {
   GemmInstance g;
   cublasContext* blas = nullptr;
@@ -130,6 +142,8 @@ struct GemmRunArgs {
   GemmInstance g;
   bool split = false;
   GemmSplit sp;
+  int* ctr = nullptr;              // device step counter (step-dependent kernel arguments)
+  cudaStream_t cap = nullptr;      // private stream for CUDA-graph capture (null: no graphs)
   cublasContext* blas = nullptr;
   bool fp64 = false;
   int Kdense = 0, D = 0, E = 0, nt = 0, obs_t0 = 0, store_every = 0, diag = 0;
@@ -146,13 +160,20 @@ int gemm_propagate(const GemmRunArgs& a, cudaStream_t st);
 // FP32 pieces of the GEMM schedule reused by the split-precision one
 void gemm_init_split(const GemmInstance& g, const double2* rho0, cudaStream_t st);
 void gemm_obs_split(const GemmInstance& g, int E, double2* obs_out, cudaStream_t st);
-void gemm_drive_split(const GemmInstance& g, int D, const double* f, int nt, int step, cudaStream_t st);
+void gemm_drive_split(const GemmInstance& g, int D, const double* f, int nt, const int* ctr, cudaStream_t st);
+void gemm_step_inc(int* ctr, cudaStream_t st);
+// nt RK4 steps: eagerly, or as CUDA graphs of up to 16 steps captured once on
+// `cap` and replayed on `st` (one_step launches one step on the stream given)
+template <typename F>
+int run_steps(int nt, cudaStream_t st, cudaStream_t cap, F&& one_step);
 // split-precision schedule (lgb_gemm_tc.cu)
 int split_padded_dim(int N);
 size_t split_partial_slots(int N);
 size_t split_tpart_elems(int NP, int Kd, int n_sm, bool bf16);
 size_t split_rpart_elems(int NP, int Kd, int n_sm, bool bf16);
 int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_sm, cudaStream_t st);
+// split-K factors of one instance for a CTA budget (SM count x waves)
+void split_set_ksplit(GemmSplit& sp, int Kd, int cta_budget);
 int split_propagate(const GemmRunArgs& a, cudaStream_t st);
 
 }  // namespace lgb
@@ -169,6 +190,11 @@ struct lgb_plan {
   std::vector<int> order_w;                // 384-thread FP32 CTA-kernel instances (64 < N <= 76)
   std::vector<int> tc_order;               // tensor-core kernel instances, largest first
   int tc_smem = 0;
+  int opt_pairs = 1;                       // LGB_OPT_TC_PAIRS
+  int opt_waves = 1;                       // LGB_OPT_GEMM_WAVES
+  cudaStream_t cap_stream = nullptr;       // GEMM schedule: CUDA-graph capture
+  int* d_ctr = nullptr;                    // GEMM schedule: device step counter
+  void* blas_ws = nullptr;                 // cuBLAS workspace (graph capture allocates nothing)
   int smem_w = 0;
   int n_sm = 0;
   cudaStream_t side[2] = {nullptr, nullptr};  // streams for kernels that run beside the first
@@ -219,3 +245,45 @@ struct lgb_plan {
   std::vector<lgb::GemmSplit> gsplit;     // split-precision operands (3xTF32 / 3xBF16 GEMM schedule)
   double2* d_gtmp = nullptr;
 };
+
+// ---- CUDA-graph step runner of the GEMM schedule (header-defined template) -------
+namespace lgb {
+template <typename F>
+int run_steps(int nt, cudaStream_t st, cudaStream_t cap, F&& one_step) {
+  constexpr int kGraphSteps = 16, kGraphMin = 32;
+  if (cap == nullptr || nt < kGraphMin) {
+    for (int s = 0; s < nt; ++s) {
+      const int r = one_step(st);
+      if (r != LGB_OK) return r;
+    }
+    return LGB_OK;
+  }
+  // capture `steps` steps on the private stream (nothing executes there) and
+  // replay the instantiated graph on the caller's stream
+  auto build = [&](int steps, cudaGraphExec_t* ex) -> int {
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LGB_ERR_CUDA;
+    int r = LGB_OK;
+    for (int s = 0; s < steps && r == LGB_OK; ++s) r = one_step(cap);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cap, &g);
+    if (r != LGB_OK || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return r != LGB_OK ? r : LGB_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(ex, g, 0);
+    cudaGraphDestroy(g);
+    return ei == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+  };
+  const int S = nt < kGraphSteps ? nt : kGraphSteps;
+  cudaGraphExec_t full = nullptr, rest = nullptr;
+  int r = build(S, &full);
+  if (r == LGB_OK && nt % S) r = build(nt % S, &rest);
+  for (int k = 0; k < nt / S && r == LGB_OK; ++k)
+    if (cudaGraphLaunch(full, st) != cudaSuccess) r = LGB_ERR_CUDA;
+  if (r == LGB_OK && rest != nullptr && cudaGraphLaunch(rest, st) != cudaSuccess) r = LGB_ERR_CUDA;
+  // an executable graph destroyed while in flight is freed when it completes
+  if (full) cudaGraphExecDestroy(full);
+  if (rest) cudaGraphExecDestroy(rest);
+  return r;
+}
+}  // namespace lgb

@@ -671,14 +671,15 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
     __syncthreads();
     if (item >= n_items) break;
     const int b = order[item];
-    if (p.npad[b] <= 32) {
+    if (p.npad[b] <= 32 && p.tc_pairs) {
       small = item;
       break;
     }
-    if (p.npad[b] == 48) {
-      tc_instance<BF16, 48, 1>(p, b, smem, sh, 0, phase, alive);
-    } else {
-      tc_instance<BF16, 64, 1>(p, b, smem, sh, 0, phase, alive);
+    switch (p.npad[b]) {
+      case 16: tc_instance<BF16, 16, 1>(p, b, smem, sh, 0, phase, alive); break;
+      case 32: tc_instance<BF16, 32, 1>(p, b, smem, sh, 0, phase, alive); break;
+      case 48: tc_instance<BF16, 48, 1>(p, b, smem, sh, 0, phase, alive); break;
+      default: tc_instance<BF16, 64, 1>(p, b, smem, sh, 0, phase, alive); break;
     }
   }
   // NP <= 32: the warps of TMEM lane quarters 0-1 and those of quarters 2-3

@@ -115,6 +115,12 @@ class Propagator:
         except Exception:
             pass
 
+    def set_option(self, name, value):
+        """Tuning option of the plan (``lgb_plan_set_option``): ``tc_pairs``
+        (0/1) or ``gemm_waves`` (1/2)."""
+        C.check(self._lib.lgb_plan_set_option(self._plan, C.OPT[name], int(value)),
+                "lgb_plan_set_option")
+
     def info(self):
         inf = C.PlanInfo()
         C.check(self._lib.lgb_plan_get_info(self._plan, ctypes.byref(inf)), "lgb_plan_get_info")

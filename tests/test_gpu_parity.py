@@ -334,3 +334,25 @@ def test_gemm_schedule_driven_vs_oracle(prec, tol):
         obs, states = O.lindblad_driven([H0[b], [mu[b], E]], rho0[b], cops[b], [mu[b]], Nt=8, dt=0.02)
         assert np.abs(res["rho"][b] - states[-1]).max() < tol
         assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < tol * 10
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32), ("3xtf32", TOL32)])
+def test_gemm_schedule_graph_replay_vs_oracle(prec, tol):
+    """45 steps: two replays of a captured 16-step CUDA graph and one of a
+    13-step one, with a drive term, stored states and the t0 observable row
+    (all step-dependent outputs resolved from the device step counter)."""
+    rng = np.random.default_rng(33)
+    N, nt, dt = 100, 45, 0.01
+    E = W.gp_pulse(nt, dt, seed=5, amp=0.3)
+    H0, mu = W.gue_matrix(rng, N), W.gue_matrix(rng, N)
+    cops = [(rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) * 0.02 for _ in range(2)]
+    rho0 = np.eye(N, dtype=complex) / N
+    res = propagate_batch([H0], [cops], [rho0], dt, nt, e_ops=[[mu]], obs_t0=True, store_every=7,
+                          precision=prec, schedule="gemm", drive_ops=[[mu]], drive=E[None, :])
+    assert res["info"]["schedule"] == "gemm"
+    obs, states = O.lindblad_driven([H0, [mu, E]], rho0, cops, [mu], Nt=nt, dt=dt)
+    assert np.abs(res["rho"][0] - states[-1]).max() < tol
+    for k in range(nt // 7):
+        assert np.abs(res["states"][0][k] - states[7 * k + 6]).max() < tol
+    ref_rows = np.concatenate([[[np.trace(mu @ rho0)]], obs], axis=0)
+    assert np.abs(res["observables"][0] - ref_rows).max() < tol * 10
