@@ -183,10 +183,15 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
  *                      CTA when NP <= 32, 0 one at a time
  *   LGB_OPT_GEMM_WAVES split-precision GEMM schedule: the split-K factors fill
  *                      1 (default) or 2 waves of CTAs on the SMs
+ *   LGB_OPT_TEST_STALL test hook of the error path: 1 makes the tensor-core
+ *                      kernel skip its first MMA commit, so that its bounded
+ *                      wait (4096 polls) runs out and every instance it was
+ *                      given reports LGB_ERR_TIMEOUT; nothing faults or hangs
  * Returns LGB_ERR_INVALID_ARG for an unknown option or value. */
 typedef enum {
   LGB_OPT_TC_PAIRS = 1,
-  LGB_OPT_GEMM_WAVES = 2
+  LGB_OPT_GEMM_WAVES = 2,
+  LGB_OPT_TEST_STALL = 3
 } lgb_option_t;
 
 int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value);

@@ -42,7 +42,7 @@ EXPORTS = [
     "lgb_propagate_noalloc", "lgb_plan_adjoint", "lgb_plan_set_option",
 ]
 # tuning options (lgb_option_t)
-OPT = {"tc_pairs": 1, "gemm_waves": 2}
+OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3}
 FLAG_ADJOINT = 1
 
 

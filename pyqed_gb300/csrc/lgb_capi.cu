@@ -448,6 +448,8 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
   plan->last_stream = st;
   CtaParams p{};
   p.tc_pairs = plan->opt_pairs;
+  p.test_stall = plan->opt_stall;
+  p.spin = plan->opt_stall ? 4096 : 0;  // the test hook's waits give up after 4096 polls
   p.n_inst = pr.n_inst;
   p.n_cops = pr.n_cops;
   p.cops_kind = pr.cops_kind;
@@ -679,6 +681,10 @@ int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value) {
       for (auto& q : plan->gsplit) lgb::split_set_ksplit(q, Kd, plan->n_sm * value);
       return LGB_OK;
     }
+    case LGB_OPT_TEST_STALL:
+      if (value != 0 && value != 1) return LGB_ERR_INVALID_ARG;
+      plan->opt_stall = value;
+      return LGB_OK;
     default:
       return LGB_ERR_INVALID_ARG;
   }

@@ -87,6 +87,8 @@ struct CtaParams {
   void* ystore;              // optional: every stage input, 4 * ycap x NP x NPS per instance
   int ycap;                  // steps held per instance in ystore
   int tc_pairs;              // tensor-core kernel: two instances per CTA for NP <= 32
+  int test_stall;            // test hook: the first MMA commit is never issued
+  long long spin;            // poll bound of the tensor-core kernel's waits (0: default)
 };
 
 }  // namespace lgb

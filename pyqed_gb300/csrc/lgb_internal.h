@@ -192,6 +192,7 @@ struct lgb_plan {
   int tc_smem = 0;
   int opt_pairs = 1;                       // LGB_OPT_TC_PAIRS
   int opt_waves = 1;                       // LGB_OPT_GEMM_WAVES
+  int opt_stall = 0;                       // LGB_OPT_TEST_STALL
   cudaStream_t cap_stream = nullptr;       // GEMM schedule: CUDA-graph capture
   int* d_ctr = nullptr;                    // GEMM schedule: device step counter
   void* blas_ws = nullptr;                 // cuBLAS workspace (graph capture allocates nothing)

@@ -424,12 +424,13 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   };
 
   // Bounded wait for the last commit; on time-out mark the instance and stop.
+  const long long spin = p.spin > 0 ? p.spin : kSpinLimit;
   auto wait_mma = [&]() -> bool {
-    const bool ok = mbar_wait(mbar, phase, kSpinLimit);
+    const bool ok = mbar_wait(mbar, phase, spin);
     phase ^= 1u;
     if (gor<GR>(grp, !ok)) {
       if (tid == 0) p.err[b] = 5;  // LGB_ERR_TIMEOUT
-      mbar_wait(mbar, phase ^ 1u, kSpinLimit);
+      mbar_wait(mbar, phase ^ 1u, spin);  // MMAs still in flight finish before TMEM is freed
       alive = false;
       return false;
     }
@@ -506,7 +507,9 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
 #pragma unroll 1
     for (int stage = 0; stage < 4; ++stage) {
       sync_for_mma<GR>(grp);
-      if (tid == 0) {
+      // (test hook: with test_stall the first stage's MMAs and commit are not
+      // issued, so that its bounded wait runs out)
+      if (tid == 0 && !(p.test_stall && step == 0 && stage == 0)) {
         fence_after_sync();
         issue_stage<BF16, NP>(tmem_d, sbase, mshift);
         mma_commit(mbar);
@@ -664,13 +667,18 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
   bool alive = true;
   int small = -1;
   // Instances with NP >= 48 (the queue is sorted by size): the whole CTA.
-  while (alive) {
+  while (true) {
     if (tid == 0) sh.next[0] = atomicAdd(queue, 1);
     __syncthreads();
     const int item = sh.next[0];
     __syncthreads();
     if (item >= n_items) break;
     const int b = order[item];
+    if (!alive) {
+      // after a timed-out wait this CTA only marks the instances it takes
+      if (tid == 0) p.err[b] = 5;  // LGB_ERR_TIMEOUT
+      continue;
+    }
     if (p.npad[b] <= 32 && p.tc_pairs) {
       small = item;
       break;
@@ -693,7 +701,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
     uint32_t ph = g == 0 ? phase : 0u;
     int item = g == 0 ? small : -1;
     bool galive = true;
-    while (galive) {
+    while (true) {
       if (item < 0) {
         if ((tid & 0x1bf) == 0) sh.next[g] = atomicAdd(queue, 1);  // warp 0 / 2, lane 0
         gsync<2>(g);
@@ -702,6 +710,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
       }
       if (item >= n_items) break;
       const int b = order[item];
+      if (!galive) {
+        if ((tid & 0x1bf) == 0) p.err[b] = 5;  // LGB_ERR_TIMEOUT (not propagated)
+        item = -1;
+        continue;
+      }
       if (p.npad[b] == 16) {
         tc_instance<BF16, 16, 2>(p, b, sg, sh, g, ph, galive);
       } else {

@@ -116,8 +116,8 @@ class Propagator:
             pass
 
     def set_option(self, name, value):
-        """Tuning option of the plan (``lgb_plan_set_option``): ``tc_pairs``
-        (0/1) or ``gemm_waves`` (1/2)."""
+        """Option of the plan (``lgb_plan_set_option``): ``tc_pairs`` (0/1),
+        ``gemm_waves`` (1/2), or the error-path test hook ``test_stall`` (0/1)."""
         C.check(self._lib.lgb_plan_set_option(self._plan, C.OPT[name], int(value)),
                 "lgb_plan_set_option")
 

@@ -356,3 +356,39 @@ def test_gemm_schedule_graph_replay_vs_oracle(prec, tol):
         assert np.abs(res["states"][0][k] - states[7 * k + 6]).max() < tol
     ref_rows = np.concatenate([[[np.trace(mu @ rho0)]], obs], axis=0)
     assert np.abs(res["observables"][0] - ref_rows).max() < tol * 10
+
+
+def test_bounded_wait_timeout_is_reported_and_context_survives():
+    """Error path of the tensor-core kernel's bounded waits: with the test hook
+    the first MMA commit is never issued, the wait gives up after 4096 polls,
+    every instance reports LGB_ERR_TIMEOUT (5), and the context keeps working."""
+    from pyqed_gb300.engine import Propagator
+    from pyqed_gb300.batch import prepare_batch
+    import torch
+    ex = W.exciton_batch(n_inst=40, nt=20)
+    cops = [[np.diag(c) for c in cd] for cd in ex["c_diag"]]
+    seeds = [m @ r for m, r in zip(ex["mu"], ex["rho_g"])]
+    bi = prepare_batch(ex["H"], cops, seeds, [[m] for m in ex["mu"]])
+    dims = bi.dims
+    tc = dims <= 64
+
+    def run(stall):
+        prop = Propagator(bi.dims, nt=20, dt=ex["dt"], n_cops=bi.n_cops, cops_kind=bi.cops_kind,
+                          n_eops=1, precision="3xtf32")
+        try:
+            prop.set_option("test_stall", stall)
+            prop.set_operators(bi.H, bi.cops, bi.eops)
+            out = prop.alloc_outputs(want_obs=True, want_rho=True)
+            prop.propagate_device(prop.to_device(bi.rho0), None, out)
+            torch.cuda.synchronize()
+            return prop.errors(), prop.unpack_obs(out[0])
+        finally:
+            prop.close()
+    err, _ = run(1)
+    assert np.all(err[tc] == 5) and np.all(err[~tc] == 0)
+    err, obs = run(0)
+    assert np.all(err == 0)
+    b = int(np.argmax(tc))
+    ref = O.propagate_diag_correlation(ex["H"][b], ex["mu"][b], ex["rho_g"][b], ex["c_diag"][b],
+                                       ex["dt"], 20)
+    assert np.abs(obs[b, :, 0] - ref).max() < 1e-5 * np.abs(ref).max()
