@@ -24,7 +24,7 @@ import numpy as np
 __all__ = [
     "jaynes_cummings", "gue_matrix", "gue_instance", "exciton_dims",
     "exciton_instance", "exciton_batch", "gp_pulse", "driven_batch",
-    "WORKLOADS",
+    "ohmic_spectrum", "redfield_chain", "WORKLOADS",
 ]
 
 
@@ -182,3 +182,39 @@ WORKLOADS = {
     "gue1024": "GUE N=1024, K=8 dense collapse ops, rank-4 rho0, dt=0.005, 1000 steps",
     "driven256": "256 driven instances N=64, K=2, H(t)=H0-E(t)mu, dt=0.01, 2000 steps",
 }
+
+
+class ohmic_spectrum:
+    """Bath spectral function for the Redfield tensor: Ohmic density with an
+    exponential cutoff at inverse temperature beta,
+        S(w) = 2 eta w exp(-|w| / wc) / (1 - exp(-beta w)),   S(0) = 2 eta / beta,
+    so that S(w) / S(-w) = exp(beta w) (detailed balance).  A picklable
+    callable of one float, as ``RedfieldSolver(spectra=[...])`` expects."""
+
+    def __init__(self, eta=0.05, wc=0.5, beta=5.0):
+        self.eta, self.wc, self.beta = float(eta), float(wc), float(beta)
+
+    def __call__(self, w):
+        w = float(w)
+        if abs(w) < 1e-12:
+            return 2.0 * self.eta / self.beta
+        return 2.0 * self.eta * w * np.exp(-abs(w) / self.wc) / (1.0 - np.exp(-self.beta * w))
+
+
+def redfield_chain(n=6, seed=7, e0=0.0, sigma=0.05, J=0.02, eta=0.05, wc=0.5, beta=5.0):
+    """Disordered exciton chain (single-excitation manifold, N = n sites) with
+    one independent Ohmic bath per site: a_ops = |k><k|, the Redfield setting
+    of ``pyqed/oqs.py:30-100``.  rho0 = |n-1><n-1|; e_ops = the site populations
+    of the first and last site."""
+    rng = np.random.default_rng(seed)
+    H = np.diag(e0 + sigma * rng.standard_normal(n) + 0.08 * np.arange(n)).astype(complex)
+    k = np.arange(n - 1)
+    H[k, k + 1] = J
+    H[k + 1, k] = J
+    a_ops = [np.diag((np.arange(n) == s).astype(complex)) for s in range(n)]
+    rho0 = np.zeros((n, n), complex)
+    rho0[n - 1, n - 1] = 1.0
+    e_ops = [a_ops[0], a_ops[n - 1]]
+    return dict(H=H, a_ops=a_ops, spectra=[ohmic_spectrum(eta, wc, beta)] * n, rho0=rho0, e_ops=e_ops,
+                eta=eta, wc=wc, beta=beta)
+

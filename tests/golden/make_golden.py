@@ -48,6 +48,41 @@ def digest(*arrays):
     return h.hexdigest()
 
 
+def redfield_fixtures(oqs):
+    out = {}
+    # 8. Redfield solver (pyqed/oqs.py:30-100, 364-459, 519-563): a disordered
+    # chain with one Ohmic bath per site, and a complex GUE Hamiltonian with
+    # two general Hermitian system-bath operators
+    ch = W.redfield_chain(n=6, seed=7)
+    sol = oqs.RedfieldSolver(ch["H"], c_ops=ch["a_ops"], spectra=ch["spectra"])
+    r = sol.evolve(ch["rho0"], dt=0.1, Nt=200, e_ops=ch["e_ops"])
+    keep = [0, 99, 199]
+    out["redfield_chain"] = dict(
+        H=ch["H"], a_ops=np.stack(ch["a_ops"]), rho0=ch["rho0"], e_ops=np.stack(ch["e_ops"]),
+        eta=ch["eta"], wc=ch["wc"], beta=ch["beta"], dt=0.1, nt=200, R=sol.R.toarray(),
+        evecs=sol.evecs, observables=r.observables, state_index=np.array(keep),
+        states=np.stack([r.rholist[k] for k in keep]))
+    rng = np.random.default_rng(8)
+    N = 8
+    H = W.gue_matrix(rng, N)
+    a_ops = []
+    for _ in range(2):
+        m = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) * 0.3
+        a_ops.append(0.5 * (m + m.conj().T))
+    spectra = [W.ohmic_spectrum(0.04, 1.0, 2.0), W.ohmic_spectrum(0.02, 0.5, 8.0)]
+    psi = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    psi /= np.linalg.norm(psi)
+    rho0 = np.outer(psi, psi.conj())
+    sol = oqs.RedfieldSolver(H, c_ops=a_ops, spectra=spectra)
+    r = sol.evolve(rho0, dt=0.05, Nt=120, e_ops=[H, a_ops[0]])
+    out["redfield_gue"] = dict(
+        H=H, a_ops=np.stack(a_ops), spectra=np.array([[0.04, 1.0, 2.0], [0.02, 0.5, 8.0]]),
+        rho0=rho0, e_ops=np.stack([H, a_ops[0]]), dt=0.05, nt=120, R=sol.R.toarray(), evecs=sol.evecs,
+        observables=r.observables, rho_last=r.rholist[-1])
+
+    return out
+
+
 def main():
     oqs = load()
     out = {}
@@ -143,6 +178,11 @@ def main():
                                              csr_matrix(a)], dt=0.02, nt=50)
     out["corr_jc"] = dict(a=a, sm=sm, c2=c2, c3=c3, c4=c4, cor_dat=np.array(cor_dat))
 
+    out.update(redfield_fixtures(oqs))
+    save(out)
+
+
+def save(out):
     for name, arrs in out.items():
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **arrs)
@@ -150,4 +190,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["redfield"]:
+        save(redfield_fixtures(load()))
+    else:
+        main()

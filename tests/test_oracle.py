@@ -112,3 +112,43 @@ def test_rhs_diag_equals_dense():
     a = O.rhs(rho, H, [np.diag(c) for c in cd])
     b = O.rhs_diag(rho, H, cd)
     assert np.abs(a - b).max() < 1e-13
+
+
+# ---- Redfield (pyqed/oqs.py:30-100, 364-459, 519-563) ------------------------------
+
+def test_redfield_oracle_matches_reference_chain(golden):
+    from oracle import redfield_oracle as RO
+    from pyqed_gb300 import workloads as W
+    g = golden("redfield_chain")
+    ch = W.redfield_chain(n=6, seed=7)
+    assert np.array_equal(ch["H"], g["H"])
+    R, V = RO.redfield_tensor(ch["H"], ch["a_ops"], ch["spectra"])
+    obs, rholist, _ = RO.redfield_propagate(R, ch["rho0"], V, int(g["nt"]), float(g["dt"]), ch["e_ops"])
+    assert np.abs(obs - g["observables"]).max() < 1e-12
+    for k, s in zip(g["state_index"], g["states"]):
+        assert np.abs(rholist[k] - s).max() < 1e-12
+    # the tensor itself, in the reference's eigenbasis
+    assert np.abs(np.abs(V.conj().T @ g["evecs"]) - np.eye(6)).max() < 1e-10
+
+
+def test_redfield_oracle_matches_reference_gue(golden):
+    from oracle import redfield_oracle as RO
+    from pyqed_gb300 import workloads as W
+    g = golden("redfield_gue")
+    spectra = [W.ohmic_spectrum(*p) for p in g["spectra"]]
+    R, V = RO.redfield_tensor(g["H"], list(g["a_ops"]), spectra)
+    obs, rholist, _ = RO.redfield_propagate(R, g["rho0"], V, int(g["nt"]), float(g["dt"]), list(g["e_ops"]))
+    assert np.abs(obs - g["observables"]).max() < 1e-12
+    assert np.abs(rholist[-1] - g["rho_last"]).max() < 1e-12
+    # element formula == kron construction
+    ev = np.linalg.eigvalsh(g["H"])
+    Wm = ev[:, None] - ev[None, :]
+    A = [V.conj().T @ a @ V for a in g["a_ops"]]
+    C = [np.vectorize(s)(-Wm) for s in spectra]
+    assert np.abs(RO.redfield_elementwise(ev, A, C) - R).max() < 1e-12
+
+
+def test_redfield_oracle_rejects_nonhermitian():
+    from oracle import redfield_oracle as RO
+    with pytest.raises(TypeError):
+        RO.redfield_tensor(np.eye(2), [np.array([[0, 1], [0, 0]], complex)], [lambda w: 1.0])
