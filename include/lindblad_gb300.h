@@ -196,6 +196,57 @@ typedef enum {
 
 int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value);
 
+/* ---- Redfield master equation ------------------------------------------------
+ * Replaces RedfieldSolver.redfield_tensor / evolve / _redfield
+ * (pyqed/oqs.py:30-100, 364-459, 519-563).  Everything lives in the
+ * eigenbasis of H; vec is row-major (vec(rho)[a*N + b] = rho[a][b]).
+ *
+ * lgb_redfield_tensor builds, for one system of dimension n with n_ops
+ * system-bath operators, the N^2 x N^2 generator (complex128, row-major)
+ *     R = -i [E, .] - sum_k [A_k, L_k . - . L_k^dag],   L_k = C_k o A_k,
+ * from the eigenvalues E (n FP64), the operators A_k = V^dag a_k V
+ * (n_ops x n x n complex128) and the bath spectra C_k[m][l] = S_k(e_l - e_m)
+ * (n_ops x n x n FP64) -- the reference's redfield_tensor (pyqed/oqs.py:519-563).
+ * All pointers are device pointers.  n <= lgb_redfield_max_dim(LGB_PREC_FP32). */
+int lgb_redfield_tensor(int32_t n, int32_t n_ops, const double* evals, const double* A,
+                        const double* C, double* R_out, void* stream);
+
+/* Largest supported dimension per precision (64 for FP32, 48 for FP64). */
+int lgb_redfield_max_dim(int32_t precision);
+
+typedef struct lgb_redfield_plan* lgb_redfield_t;
+
+typedef struct {
+  int32_t n_inst;       /* independent systems in the batch                          */
+  int32_t n_eops;       /* observables per system, <= 16                              */
+  int32_t nt;           /* RK4 steps                                                  */
+  int32_t precision;    /* LGB_PREC_FP64 or LGB_PREC_FP32                             */
+  int32_t store_every;  /* keep vec(rho) every this many steps (0: none)              */
+  int32_t reserved;     /* 0                                                          */
+  double dt;
+} lgb_redfield_problem_t;
+
+/* A batch of systems of dimensions dims[n_inst] (host array). */
+int lgb_redfield_create(lgb_redfield_t* plan, const lgb_redfield_problem_t* prob, const int32_t* dims);
+int lgb_redfield_destroy(lgb_redfield_t plan);
+
+/* Generators (packed: system b at offset sum_{c<b} N_c^4, complex128) and the
+ * observables as vec(O_e^T) in the eigenbasis (packed: system b at
+ * n_eops * sum_{c<b} N_c^2, e-major).  Device pointers. */
+int lgb_redfield_set(lgb_redfield_t plan, const double* R, const double* eops, void* stream);
+
+/* nt RK4 steps of d vec(rho)/dt = R vec(rho) (pyqed/phys.py:1051-1064).
+ *   rho0       vec(rho0) in the eigenbasis, packed (sum N^2, complex128)
+ *   obs_out    [n_inst][nt][n_eops] complex128 (Tr[O rho] after every step), or NULL
+ *   rho_out    vec(rho) after nt steps, packed, or NULL
+ *   states_out vec(rho) every store_every steps: system b holds a contiguous
+ *              block of (nt / store_every) x N_b^2 at (nt / store_every) * sum_{c<b} N_c^2
+ * A state that becomes NaN/Inf stops its system with LGB_ERR_NONFINITE
+ * (lgb_redfield_errors). */
+int lgb_redfield_propagate(lgb_redfield_t plan, const double* rho0, double* obs_out, double* rho_out,
+                           double* states_out, void* stream);
+int lgb_redfield_errors(lgb_redfield_t plan, int32_t* flags_host);
+
 /* ---- propagation without device allocation ---------------------------------
  * No counterpart in the reference: pyqed is pure Python and never manages
  * device memory.

@@ -8,8 +8,9 @@ hand-written sm_103a CUDA kernels behind the C ABI of
 from .mol import Result, load_result
 from .oqs import LindbladSolver, liouvillian
 from .batch import propagate_batch, correlation_batch
+from .redfield import RedfieldSolver, redfield_batch
 from . import workloads
 
 __all__ = ["LindbladSolver", "Result", "load_result", "liouvillian", "propagate_batch",
-           "correlation_batch", "workloads"]
+           "correlation_batch", "RedfieldSolver", "redfield_batch", "workloads"]
 __version__ = "0.1.0"

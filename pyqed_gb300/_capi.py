@@ -40,6 +40,8 @@ EXPORTS = [
     "lgb_get_version", "lgb_status_string", "lgb_plan_create", "lgb_plan_destroy",
     "lgb_plan_set_operators", "lgb_plan_propagate", "lgb_plan_errors", "lgb_plan_get_info",
     "lgb_propagate_noalloc", "lgb_plan_adjoint", "lgb_plan_set_option",
+    "lgb_redfield_tensor", "lgb_redfield_max_dim", "lgb_redfield_create", "lgb_redfield_destroy",
+    "lgb_redfield_set", "lgb_redfield_propagate", "lgb_redfield_errors",
 ]
 # tuning options (lgb_option_t)
 OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3}
@@ -69,6 +71,14 @@ class PlanInfo(ctypes.Structure):
         ("schedule", ctypes.c_int32), ("precision", ctypes.c_int32),
         ("smem_bytes", ctypes.c_int32), ("launches_per_propagate", ctypes.c_int32),
         ("workspace_bytes", ctypes.c_int64), ("flops_per_step", ctypes.c_int64),
+    ]
+
+
+class RedfieldProblem(ctypes.Structure):
+    _fields_ = [
+        ("n_inst", ctypes.c_int32), ("n_eops", ctypes.c_int32), ("nt", ctypes.c_int32),
+        ("precision", ctypes.c_int32), ("store_every", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("dt", ctypes.c_double),
     ]
 
 
@@ -111,6 +121,21 @@ def lib():
     L.lgb_plan_errors.argtypes = [vp, ctypes.POINTER(i32)]
     L.lgb_plan_get_info.restype = ctypes.c_int
     L.lgb_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+    L.lgb_redfield_tensor.restype = ctypes.c_int
+    L.lgb_redfield_tensor.argtypes = [i32, i32, dp, dp, dp, dp, vp]
+    L.lgb_redfield_max_dim.restype = ctypes.c_int
+    L.lgb_redfield_max_dim.argtypes = [i32]
+    L.lgb_redfield_create.restype = ctypes.c_int
+    L.lgb_redfield_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(RedfieldProblem),
+                                      ctypes.POINTER(i32)]
+    L.lgb_redfield_destroy.restype = ctypes.c_int
+    L.lgb_redfield_destroy.argtypes = [vp]
+    L.lgb_redfield_set.restype = ctypes.c_int
+    L.lgb_redfield_set.argtypes = [vp, dp, dp, vp]
+    L.lgb_redfield_propagate.restype = ctypes.c_int
+    L.lgb_redfield_propagate.argtypes = [vp, dp, dp, dp, dp, vp]
+    L.lgb_redfield_errors.restype = ctypes.c_int
+    L.lgb_redfield_errors.argtypes = [vp, ctypes.POINTER(i32)]
     L.lgb_plan_set_option.restype = ctypes.c_int
     L.lgb_plan_set_option.argtypes = [vp, i32, i32]
     L.lgb_plan_adjoint.restype = ctypes.c_int

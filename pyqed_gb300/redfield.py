@@ -1,0 +1,233 @@
+"""Drop-in mirror of the reference's Redfield solver on the GPU.
+
+``RedfieldSolver`` follows ``pyqed.oqs.RedfieldSolver`` (``pyqed/oqs.py:30-100``):
+same constructor (H, c_ops = the Hermitian system-bath operators, spectra =
+one callable S_k(w) per operator, e_ops), ``redfield_tensor()`` returning the
+generator as a CSR matrix and the eigenvectors (``pyqed/oqs.py:519-563``) and
+``evolve()`` returning a ``Result`` with the observables after every step and
+the states transformed back to the original basis (``_redfield``,
+``pyqed/oqs.py:364-459``).  The N^2 x N^2 generator is built on the GPU
+(``lgb_redfield_tensor``, O(N^4 K)) and propagated there by the batched RK4
+kernel (``lgb_redfield_propagate``).  The eigendecomposition of H and the
+bath spectra (Python callables) are evaluated on the host, as in the
+reference.  ``redfield_batch`` propagates many systems in one launch.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _capi as C
+from .engine import _device, to_dense
+from .mol import Result
+
+__all__ = ["RedfieldSolver", "redfield_batch", "build_tensor"]
+
+_PREC = {"fp64": C.PREC["fp64"], "fp32": C.PREC["fp32"]}
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else None
+
+
+def _herm_check(a_ops):
+    for a in a_ops:
+        if not np.allclose(a, a.conj().T):
+            raise TypeError("Operators in a_ops must be Hermitian.")
+
+
+def _eigen_parts(H, a_ops, spectra):
+    """Host part of ``redfield_tensor``: eigenbasis, A_k = V^dag a_k V and the
+    spectra C_k[m][l] = S_k(-(e_m - e_l))."""
+    H = to_dense(H)
+    a_ops = [to_dense(a) for a in a_ops]
+    _herm_check(a_ops)
+    evals, evecs = np.linalg.eigh(H)
+    W = np.real(evals[:, None] - evals[None, :])
+    N = len(evals)
+    A = np.stack([evecs.conj().T @ a @ evecs for a in a_ops]) if a_ops else np.zeros((0, N, N), complex)
+    Cs = np.stack([np.array([[float(s(-W[n, m])) for m in range(N)] for n in range(N)]) for s in spectra[:len(a_ops)]]) \
+        if a_ops else np.zeros((0, N, N))
+    return evals, evecs, A, Cs
+
+
+def build_tensor(evals, A, Cs, device=None):
+    """The generator R (device complex128, N^2 x N^2) from the eigenvalues,
+    the operators in the eigenbasis and the spectra (``lgb_redfield_tensor``)."""
+    dev = _device(device)
+    N = len(evals)
+    L = C.lib()
+    ev = torch.from_numpy(np.ascontiguousarray(evals, dtype=np.float64)).to(dev)
+    At = torch.from_numpy(np.ascontiguousarray(A, dtype=np.complex128)).to(dev)
+    Ct = torch.from_numpy(np.ascontiguousarray(Cs, dtype=np.float64)).to(dev)
+    R = torch.empty(N ** 4, dtype=torch.complex128, device=dev)
+    with torch.cuda.device(dev):
+        C.check(L.lgb_redfield_tensor(N, len(A), _ptr(ev), _ptr(At), _ptr(Ct), _ptr(R),
+                                      ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)),
+                "lgb_redfield_tensor")
+    return R
+
+
+class _Plan:
+    def __init__(self, dims, nt, dt, n_eops, precision, store_every, device):
+        self.dev = _device(device)
+        self.dims = np.asarray(dims, dtype=np.int32)
+        self.L = C.lib()
+        prob = C.RedfieldProblem(n_inst=len(dims), n_eops=n_eops, nt=nt, precision=_PREC[precision],
+                                 store_every=store_every, reserved=0, dt=dt)
+        self.plan = ctypes.c_void_p()
+        with torch.cuda.device(self.dev):
+            C.check(self.L.lgb_redfield_create(ctypes.byref(self.plan), ctypes.byref(prob),
+                                               (ctypes.c_int32 * len(dims))(*self.dims.tolist())),
+                    "lgb_redfield_create")
+        self.nt, self.n_eops, self.store_every = nt, n_eops, store_every
+        self.voff = np.concatenate([[0], np.cumsum(self.dims.astype(np.int64) ** 2)])
+
+    def stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def close(self):
+        if self.plan.value:
+            self.L.lgb_redfield_destroy(self.plan)
+            self.plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, R, Ot):
+        with torch.cuda.device(self.dev):
+            C.check(self.L.lgb_redfield_set(self.plan, _ptr(R), _ptr(Ot), self.stream()), "lgb_redfield_set")
+
+    def propagate(self, r0, want_states=False):
+        n = len(self.dims)
+        z = lambda k: torch.empty(int(k), dtype=torch.complex128, device=self.dev)  # noqa: E731
+        obs = z(n * self.nt * self.n_eops) if self.n_eops else None
+        rho = z(self.voff[-1])
+        ns = self.nt // self.store_every if self.store_every else 0
+        st = z(ns * self.voff[-1]) if (want_states and ns) else None
+        with torch.cuda.device(self.dev):
+            C.check(self.L.lgb_redfield_propagate(self.plan, _ptr(r0), _ptr(obs), _ptr(rho), _ptr(st),
+                                                  self.stream()), "lgb_redfield_propagate")
+        flags = (ctypes.c_int32 * n)()
+        self.L.lgb_redfield_errors(self.plan, flags)
+        bad = [i for i in range(n) if flags[i]]
+        if bad:
+            raise C.LindbladError(int(flags[bad[0]]), "system %d" % bad[0])
+        return obs, rho, st
+
+
+class RedfieldSolver:
+    """``pyqed.oqs.RedfieldSolver`` on the GPU (``pyqed/oqs.py:30-100``)."""
+
+    def __init__(self, H, c_ops=None, spectra=None, e_ops=None):
+        self.H = H
+        self.c_ops = c_ops
+        self.R = None
+        self.spectra = spectra
+        self.evecs = None
+        self.dim = H.shape[0]
+        self.U = None
+        self.G = None
+        self.e_ops = e_ops
+        self._Rdev = None
+
+    def idm(self, sp=True):
+        """vec of the identity in Liouville space (row-major)."""
+        from scipy.sparse import csr_matrix
+        v = np.eye(self.dim).flatten()
+        return csr_matrix(v.reshape(-1, 1)) if sp else v
+
+    def configure(self, H, c_ops, e_ops):
+        self.c_ops = c_ops
+        self.e_ops = e_ops
+        self.H = H
+        self.R = None
+        self._Rdev = None
+
+    def redfield_tensor(self, secular=False):
+        """(R as CSR, eigenvectors), ``pyqed/oqs.py:519-563``; R is built on the GPU."""
+        from scipy.sparse import csr_matrix
+        if self.spectra is None:
+            raise TypeError('Specify the bath spectral function.')
+        evals, evecs, A, Cs = _eigen_parts(self.H, self.c_ops or [], self.spectra)
+        self._Rdev = build_tensor(evals, A, Cs)
+        N = len(evals)
+        self.R = csr_matrix(self._Rdev.cpu().numpy().reshape(N * N, N * N))
+        self.evecs = evecs
+        return self.R, evecs
+
+    def evolve(self, rho0, dt, Nt, evecs=None, e_ops=[], store_states=False, t0=0, nout=1, *,
+               precision="fp64"):
+        """``_redfield`` (``pyqed/oqs.py:364-459``): Result with the
+        observables Tr[O rho] after every step (Nt rows) and rholist, the Nt
+        states in the original basis."""
+        if self.R is None or self._Rdev is None:
+            self.redfield_tensor()
+        V = self.evecs
+        N = V.shape[0]
+        e_ops = [] if e_ops is None else list(e_ops)
+        r0 = V.conj().T @ to_dense(rho0) @ V
+        es = [V.conj().T @ to_dense(e) @ V for e in e_ops]
+        plan = _Plan([N], Nt, dt, len(es), precision, 1 if Nt > 0 else 0, None)
+        try:
+            Ot = torch.from_numpy(np.concatenate([e.T.flatten() for e in es]) if es
+                                  else np.zeros(0, complex)).to(plan.dev)
+            plan.set(self._Rdev.to(plan.dev), Ot)
+            r0d = torch.from_numpy(np.ascontiguousarray(r0.flatten())).to(plan.dev)
+            obs, rho, st = plan.propagate(r0d, want_states=Nt > 0)
+        finally:
+            plan.close()
+        result = Result(dt=dt, Nt=Nt, rho0=r0, t0=t0)
+        result.observables = obs.cpu().numpy().reshape(Nt, len(es)) if obs is not None \
+            else np.zeros((Nt, 0), complex)
+        if st is not None:
+            Vt = torch.from_numpy(V).to(st.device)
+            S = st.reshape(Nt, N, N)
+            result.rholist = list((Vt @ S @ Vt.conj().T).cpu().numpy())
+        else:
+            result.rholist = []
+        return result
+
+
+def redfield_batch(H, a_ops, spectra, rho0, dt, Nt, e_ops=None, *, precision="fp32", store_every=0,
+                   device=None):
+    """Many Redfield systems in one launch.  H, a_ops, spectra, rho0, e_ops:
+    per-system lists.  Returns dict(observables list of (Nt, E), rho list
+    (original basis), states list of (Nt / store_every, N, N) or None)."""
+    n = len(H)
+    e_ops = e_ops if e_ops is not None else [[] for _ in range(n)]
+    E = len(e_ops[0]) if n else 0
+    parts = [_eigen_parts(H[b], a_ops[b], spectra[b]) for b in range(n)]
+    dims = [len(p[0]) for p in parts]
+    plan = _Plan(dims, Nt, dt, E, precision, store_every, device)
+    try:
+        R = torch.cat([build_tensor(p[0], p[2], p[3], plan.dev) for p in parts])
+        Ot = np.concatenate([np.concatenate([(p[1].conj().T @ to_dense(e) @ p[1]).T.flatten()
+                                             for e in e_ops[b]]) if E else np.zeros(0, complex)
+                             for b, p in enumerate(parts)])
+        plan.set(R, torch.from_numpy(Ot).to(plan.dev))
+        r0 = np.concatenate([(p[1].conj().T @ to_dense(rho0[b]) @ p[1]).flatten() for b, p in enumerate(parts)])
+        obs, rho, st = plan.propagate(torch.from_numpy(r0).to(plan.dev), want_states=store_every > 0)
+    finally:
+        plan.close()
+    res = dict(observables=[], rho=[], states=None)
+    oh = obs.cpu().numpy().reshape(n, Nt, E) if obs is not None else np.zeros((n, Nt, 0), complex)
+    rh = rho.cpu().numpy()
+    for b, p in enumerate(parts):
+        N, V = dims[b], p[1]
+        res["observables"].append(oh[b])
+        res["rho"].append(V @ rh[plan.voff[b]:plan.voff[b + 1]].reshape(N, N) @ V.conj().T)
+    if st is not None:
+        sh = st.cpu().numpy()
+        ns = Nt // store_every
+        res["states"] = []
+        for b, p in enumerate(parts):
+            N, V = dims[b], p[1]
+            blk = sh[ns * plan.voff[b]: ns * plan.voff[b + 1]].reshape(ns, N, N)
+            res["states"].append(V @ blk @ V.conj().T)
+    return res
