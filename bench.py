@@ -292,6 +292,8 @@ def run_gpu(args):
         line["adjoint"] = measure_adjoint(args, dev)
     if not args.no_large_n:
         line["large_n"] = measure_large_n(args, dev)
+    if not args.no_redfield:
+        line["redfield"] = measure_redfield(args, dev)
     # CPU baseline (oracle port of the reference's dense algorithm) and accuracy
     if not args.no_cpu:
         line["cpu_baseline"], line["accuracy"] = cpu_baseline_and_accuracy(
@@ -403,6 +405,65 @@ def measure_large_n(args, dev):
                          reference="FP64 GPU GEMM schedule, 10 steps")
     out["note"] = ("split paths: hand-written TMA + tcgen05 complex GEMMs (lgb_gemm_tc.cu); "
                    "fp32: cuBLAS CGEMM, pedantic math; algorithmic 64(1+K)N^3 flops per step")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Redfield (pyqed/oqs.py:30-100, 364-459, 519-563): batched systems
+# ---------------------------------------------------------------------------
+def measure_redfield(args, dev, n_inst=2048, n=8, nt=1000, dt=0.1):
+    """2048 disordered chains (N = 8, one Ohmic bath per site), 1000 RK4 steps
+    of vec(rho) with the 64 x 64 generator: instance-steps/s per precision
+    (CUDA events, generators resident), the generator build time, and the
+    oracle's numpy rate for the same algorithm on a sample."""
+    import torch
+    from pyqed_gb300 import workloads as W
+    from pyqed_gb300.redfield import _Plan, _eigen_parts, build_tensor
+    chains = [W.redfield_chain(n=n, seed=100 + b) for b in range(n_inst)]
+    parts = [_eigen_parts(c["H"], c["a_ops"], c["spectra"]) for c in chains]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    R = torch.cat([build_tensor(p[0], p[2], p[3], dev) for p in parts])
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    Ot = np.concatenate([np.concatenate([(p[1].conj().T @ e @ p[1]).T.flatten() for e in c["e_ops"]])
+                         for c, p in zip(chains, parts)])
+    r0 = np.concatenate([(p[1].conj().T @ c["rho0"] @ p[1]).flatten() for c, p in zip(chains, parts)])
+    M = n * n
+    flops = 32 * M * M  # 4 stages x complex GEMV (8 real flops per complex MAC)
+    out = dict(workload="redfield_chain%d x %d" % (n, n_inst), N=n, n_inst=n_inst, nt=nt, dt=dt)
+    for prec in ("fp32", "fp64"):
+        plan = _Plan([n] * n_inst, nt, dt, 2, prec, 0, dev)
+        plan.set(R, torch.from_numpy(Ot).to(dev))
+        r0d = torch.from_numpy(r0).to(dev)
+        plan.propagate(r0d)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plan.propagate(r0d)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        plan.close()
+        out[prec] = dict(seconds=t, instance_steps_per_s=n_inst * nt / t,
+                         tflops=flops * n_inst * nt / t / 1e12)
+    out["tensor_build_seconds"] = t_build
+    if not args.no_cpu:
+        from oracle import redfield_oracle as RO
+        sample, steps = 16, 50
+        # propagation only (the tensor builds are excluded above)
+        cpu_t = 0.0
+        for c in chains[:sample]:
+            Rr, V = RO.redfield_tensor(c["H"], c["a_ops"], c["spectra"])
+            y = (V.conj().T @ c["rho0"] @ V).flatten()
+            t1 = time.perf_counter()
+            for _ in range(steps):
+                y = RO.rk4_vec(y, Rr, dt)
+            cpu_t += time.perf_counter() - t1
+        out["cpu_baseline"] = dict(instance_steps_per_s=sample * steps / cpu_t, kind="port",
+                                   sample="%d chains x %d RK4 steps, numpy complex128" % (sample, steps))
+    out["note"] = ("one CTA per system, generator (64 x 64, FP32 32 KB / FP64 64 KB) in shared "
+                   "memory, warp-per-row GEMV per stage; flops = 32 N^4 per instance-step")
     return out
 
 
@@ -534,6 +595,8 @@ def main():
                     help="time only the adjoint (fwd + bwd) on the driven workload")
     ap.add_argument("--adj-n-inst", type=int, default=256)
     ap.add_argument("--adj-nt", type=int, default=2000)
+    ap.add_argument("--no-redfield", action="store_true",
+                    help="skip the batched Redfield section")
     ap.add_argument("--no-large-n", action="store_true",
                     help="skip the single large-instance (GEMM schedule) section")
     ap.add_argument("--large-nt", type=int, default=100)
