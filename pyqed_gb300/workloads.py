@@ -218,3 +218,45 @@ def redfield_chain(n=6, seed=7, e0=0.0, sigma=0.05, J=0.02, eta=0.05, wc=0.5, be
     return dict(H=H, a_ops=a_ops, spectra=[ohmic_spectrum(eta, wc, beta)] * n, rho0=rho0, e_ops=e_ops,
                 eta=eta, wc=wc, beta=beta)
 
+
+
+def heom_spin_boson(delta=1.0, eps0=1.0):
+    """Spin-boson setting of the reference's HEOM example: H = -delta/2 sx -
+    eps0/2 sz, bath coupling sz, rho0 = |1><1|, e_ops = [sz]."""
+    sx = np.array([[0, 1], [1, 0]], dtype=complex)
+    sz = np.array([[1, 0], [0, -1]], dtype=complex)
+    H = -0.5 * delta * sx - 0.5 * eps0 * sz
+    rho0 = np.zeros((2, 2), complex)
+    rho0[1, 1] = 1.0
+    return dict(H=H, sz=sz, rho0=rho0, e_ops=[sz])
+
+
+def heom_chain(n=6, seed=11, sigma=0.05, J=0.1):
+    """Disordered n-site chain coupled to one bath through the collective
+    coordinate sz = diag(linspace(1, -1, n)) (the reference's HEOM takes one
+    system-bath operator); rho0 = |0><0|, e_ops = populations of the first and
+    last site."""
+    rng = np.random.default_rng(seed)
+    H = np.diag(sigma * rng.standard_normal(n) + 0.05 * np.arange(n)).astype(complex)
+    k = np.arange(n - 1)
+    H[k, k + 1] = J
+    H[k + 1, k] = J
+    sz = np.diag(np.linspace(1.0, -1.0, n)).astype(complex)
+    rho0 = np.zeros((n, n), complex)
+    rho0[0, 0] = 1.0
+    e_ops = [np.diag((np.arange(n) == 0).astype(complex)), np.diag((np.arange(n) == n - 1).astype(complex))]
+    return dict(H=H, sz=sz, rho0=rho0, e_ops=e_ops)
+
+
+def heom_ensemble(n_inst=4096, n=8, seed=13):
+    """Parameter sweep for the batched HEOM: n_inst disordered n-site chains
+    (``heom_chain`` with per-instance seeds), each with its own bath:
+    temperature ~ U[0.5, 2], cutoff ~ U[0.2, 1], reorganization ~ U[0.01, 0.05]."""
+    rng = np.random.default_rng(seed)
+    T = rng.uniform(0.5, 2.0, n_inst)
+    cut = rng.uniform(0.2, 1.0, n_inst)
+    lam = rng.uniform(0.01, 0.05, n_inst)
+    seeds = rng.integers(0, 2 ** 31, n_inst)
+    chains = [heom_chain(n, int(s)) for s in seeds]
+    return dict(H=[c["H"] for c in chains], sz=[c["sz"] for c in chains], rho0=[c["rho0"] for c in chains],
+                e_ops=[c["e_ops"] for c in chains], temperature=T, cutoff=cut, reorganization=lam)

@@ -22,6 +22,11 @@ inputs) and the outputs of the reference's own entry points:
 * ``corr_jc.npz``    ``correlation_2op_1t``, ``correlation_3op_1t`` and
                      ``correlation_4op_1t`` (``pyqed/oqs.py:1193-1312``) on the
                      Jaynes-Cummings system, 50 steps.
+* ``redfield_*.npz`` ``RedfieldSolver.redfield_tensor`` / ``evolve``.
+* ``heom_*.npz``     ``HEOMSolver.run`` (``_heom``) on the reference's
+                     spin-boson example and a 6-site chain, and
+                     ``HEOMSolver.propagator`` (``_heom_propagator``) on a
+                     3-site chain.
 """
 from __future__ import annotations
 
@@ -80,6 +85,44 @@ def redfield_fixtures(oqs):
         rho0=rho0, e_ops=np.stack([H, a_ops[0]]), dt=0.05, nt=120, R=sol.R.toarray(), evecs=sol.evecs,
         observables=r.observables, rho_last=r.rholist[-1])
 
+    return out
+
+
+def heom_fixtures(oqs):
+    import contextlib
+    import io
+    out = {}
+    # 9. HEOM (pyqed/oqs.py:1332-1371, 1808-1935); the reference prints its
+    # bath parameters, which are discarded here
+    quiet = contextlib.redirect_stdout(io.StringIO())
+    sb = W.heom_spin_boson()
+    runs = [dict(temperature=600.0, cutoff=5.0, reorganization=0.2, nado=5, dt=0.02, nt=100),
+            dict(temperature=1.0, cutoff=0.5, reorganization=0.2, nado=8, dt=0.02, nt=400)]
+    obs = []
+    with quiet:
+        for r in runs:
+            sol = oqs.HEOMSolver(sb["H"], c_ops=[sb["sz"]], e_ops=sb["e_ops"])
+            obs.append(sol.run(rho0=sb["rho0"].real.copy(), **r))
+    out["heom_spinboson"] = dict(
+        H=sb["H"], sz=sb["sz"], rho0=sb["rho0"], e_ops=np.stack(sb["e_ops"]),
+        params=np.array([[r["temperature"], r["cutoff"], r["reorganization"], r["nado"], r["dt"], r["nt"]]
+                         for r in runs]), obs0=obs[0], obs1=obs[1])
+    ch = W.heom_chain(n=6, seed=11)
+    par = dict(temperature=1.0, cutoff=0.5, reorganization=0.03, nado=8, dt=0.01, nt=500)
+    with quiet:
+        sol = oqs.HEOMSolver(ch["H"], c_ops=[ch["sz"]], e_ops=ch["e_ops"])
+        o = sol.run(rho0=ch["rho0"], **par)
+    out["heom_chain"] = dict(H=ch["H"], sz=ch["sz"], rho0=ch["rho0"], e_ops=np.stack(ch["e_ops"]),
+                             params=np.array([par[k] for k in ("temperature", "cutoff", "reorganization",
+                                                               "nado", "dt", "nt")]), observables=o)
+    ch = W.heom_chain(n=3, seed=12)
+    par = dict(dt=0.005, nt=60, temperature=300.0, cutoff=5.0, reorganization=0.2, nado=5)
+    with quiet:
+        sol = oqs.HEOMSolver(ch["H"], c_ops=[ch["sz"]], e_ops=ch["e_ops"])
+        u = sol.propagator(**par)
+    out["heom_propagator"] = dict(H=ch["H"], sz=ch["sz"],
+                                  params=np.array([par[k] for k in ("temperature", "cutoff", "reorganization",
+                                                                    "nado", "dt", "nt")]), u=u)
     return out
 
 
@@ -179,6 +222,7 @@ def main():
     out["corr_jc"] = dict(a=a, sm=sm, c2=c2, c3=c3, c4=c4, cor_dat=np.array(cor_dat))
 
     out.update(redfield_fixtures(oqs))
+    out.update(heom_fixtures(oqs))
     save(out)
 
 
@@ -192,5 +236,7 @@ def save(out):
 if __name__ == "__main__":
     if sys.argv[1:] == ["redfield"]:
         save(redfield_fixtures(load()))
+    elif sys.argv[1:] == ["heom"]:
+        save(heom_fixtures(load()))
     else:
         main()

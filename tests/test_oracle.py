@@ -152,3 +152,47 @@ def test_redfield_oracle_rejects_nonhermitian():
     from oracle import redfield_oracle as RO
     with pytest.raises(TypeError):
         RO.redfield_tensor(np.eye(2), [np.array([[0, 1], [0, 0]], complex)], [lambda w: 1.0])
+
+
+def _heom_params(p):
+    return dict(temperature=float(p[0]), cutoff=float(p[1]), reorganization=float(p[2]), nado=int(p[3]),
+                dt=float(p[4]), nt=int(p[5]))
+
+
+def test_heom_oracle_matches_reference_spinboson(golden):
+    from oracle import heom_oracle as HO
+    g = golden("heom_spinboson")
+    sb = W.heom_spin_boson()
+    assert np.array_equal(sb["H"], g["H"]) and np.array_equal(sb["rho0"], g["rho0"])
+    for k, key in enumerate(("obs0", "obs1")):
+        o = HO.heom_run(g["H"], g["rho0"], g["sz"], list(g["e_ops"]), **_heom_params(g["params"][k]))
+        assert o.shape == g[key].shape
+        assert np.abs(o - g[key]).max() < 1e-12
+
+
+def test_heom_oracle_matches_reference_chain(golden):
+    from oracle import heom_oracle as HO
+    g = golden("heom_chain")
+    ch = W.heom_chain(n=6, seed=11)
+    assert np.array_equal(ch["H"], g["H"]) and np.array_equal(ch["sz"], g["sz"])
+    o = HO.heom_run(g["H"], g["rho0"], g["sz"], list(g["e_ops"]), **_heom_params(g["params"]))
+    assert np.abs(o - g["observables"]).max() < 1e-12
+
+
+def test_heom_oracle_matches_reference_propagator(golden):
+    from oracle import heom_oracle as HO
+    g = golden("heom_propagator")
+    p = _heom_params(g["params"])
+    u = HO.heom_propagator(g["H"], g["sz"], p["temperature"], p["cutoff"], p["reorganization"], p["nado"],
+                           p["dt"], p["nt"])
+    assert u.shape == g["u"].shape
+    assert np.abs(u - g["u"]).max() < 1e-12
+    # the propagator form and the matrix form agree on every basis state
+    N = g["H"].shape[0]
+    gamma, D0 = HO.coefficients_propagator(p["temperature"], p["cutoff"], p["reorganization"])
+    for c in range(N * N):
+        ado = np.zeros((p["nado"], N, N), complex)
+        ado[0].flat[c] = 1.0
+        for _ in range(p["nt"]):
+            HO.sweep(ado, g["H"], g["sz"], gamma, D0, p["dt"], double_first=True)
+        assert np.abs(ado.reshape(p["nado"], N * N) - g["u"][:, :, c]).max() < 1e-12
