@@ -294,6 +294,8 @@ def run_gpu(args):
         line["large_n"] = measure_large_n(args, dev)
     if not args.no_redfield:
         line["redfield"] = measure_redfield(args, dev)
+    if not args.no_heom:
+        line["heom"] = measure_heom(args, dev, n_inst=args.heom_n_inst, nt=args.heom_nt)
     # CPU baseline (oracle port of the reference's dense algorithm) and accuracy
     if not args.no_cpu:
         line["cpu_baseline"], line["accuracy"] = cpu_baseline_and_accuracy(
@@ -467,6 +469,81 @@ def measure_redfield(args, dev, n_inst=2048, n=8, nt=1000, dt=0.1):
     return out
 
 
+def heom_flops(N, nado, diag_sz=False):
+    """Algorithmic flops of one sweep (one instance-step): level 0 and level
+    nado-2 take two commutators (4 complex N^3 products), the levels between
+    three brackets whose [sz, X_{n-1}] and {sz, X_{n-1}} share sz X and X sz
+    (6 products); 8 real flops per complex multiply-add.  With a diagonal sz
+    only the two [H, X_n] products per level are N^3."""
+    L = nado
+    if diag_sz:
+        return (L - 1) * 2 * 8 * N ** 3
+    prods = 4 if L == 2 else 8 + 6 * max(0, L - 3)
+    return prods * 8 * N ** 3
+
+
+def measure_heom(args, dev, n_inst=4096, n=8, nado=8, nt=1000, dt=0.01):
+    """4096 disordered 8-site chains, each with its own Drude bath (one
+    exponential mode), an 8-level hierarchy, 1000 Euler sweeps: instance-steps/s
+    per precision (CUDA events, operators resident), and the oracle's numpy
+    rate for the reference's sweep on a sample."""
+    import torch
+    from pyqed_gb300 import workloads as W
+    from pyqed_gb300 import _capi as C
+    from pyqed_gb300.heom import _Plan, _pack, bath_run
+    e = W.heom_ensemble(n_inst, n, seed=13)
+    bath = [bath_run(e["temperature"][b], e["cutoff"][b], e["reorganization"][b]) for b in range(n_inst)]
+    coef = np.array([[g, d.real, d.imag] for g, d in bath]).ravel()
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    Hd, Sd, Cd = t(_pack(e["H"])), t(_pack(e["sz"])), t(coef)
+    Od = t(_pack([o.T for es in e["e_ops"] for o in es]))
+    r0 = t(_pack(e["rho0"]))
+    flops, flops_diag = heom_flops(n, nado), heom_flops(n, nado, diag_sz=True)
+    out = dict(workload="heom_chain%d x %d, %d levels" % (n, n_inst, nado), N=n, n_inst=n_inst, nado=nado,
+               nt=nt, dt=dt)
+    # the chains' sz is diagonal: the O(N^2) sz path; "fp32_dense_sz" times the
+    # general (dense sz) kernel on the same systems
+    for key, prec, flags in (("fp32", "fp32", C.HEOM_DIAG_SZ), ("fp64", "fp64", C.HEOM_DIAG_SZ),
+                             ("fp32_dense_sz", "fp32", 0)):
+        plan = _Plan([n] * n_inst, nt, dt, nado, 2, prec, flags, dev)
+        plan.set(Hd, Sd, Cd, Od)
+        res = plan.propagate(r0)
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            plan.propagate(r0, out=res)
+            e1.record()
+            torch.cuda.synchronize()
+            sec = e0.elapsed_time(e1) / 1e3
+            best = sec if best is None else min(best, sec)
+        plan.check_errors()
+        fl = flops_diag if flags else flops
+        out[key] = dict(seconds=best, instance_steps_per_s=n_inst * nt / best,
+                        tflops=fl * n_inst * nt / best / 1e12, layout=plan.layout())
+        plan.close()
+    if not args.no_cpu:
+        from oracle import heom_oracle as HO
+        sample, steps = 16, 100
+        cpu_t = 0.0
+        for b in range(sample):
+            ado = np.zeros((nado, n, n), complex)
+            ado[0] = e["rho0"][b]
+            t1 = time.perf_counter()
+            for _ in range(steps):
+                HO.sweep(ado, e["H"][b], e["sz"][b], bath[b][0], bath[b][1], dt)
+                [np.trace(o @ ado[0]) for o in e["e_ops"][b]]
+            cpu_t += time.perf_counter() - t1
+        out["cpu_baseline"] = dict(instance_steps_per_s=sample * steps / cpu_t, kind="port",
+                                   sample="%d chains x %d sweeps, numpy complex128" % (sample, steps))
+    out["note"] = ("one thread group per system (a warp: one thread per column and row pair), -iH, sz and "
+                   "the %d levels in shared memory, one group barrier per level; flops per instance-step = "
+                   "%d with the diagonal sz, %d with a dense sz (commutator products, 8 flops per complex "
+                   "MAC)" % (nado, flops_diag, flops))
+    return out
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline / reference arm (the oracle port; the only oracle use here)
 # ---------------------------------------------------------------------------
@@ -597,11 +674,16 @@ def main():
     ap.add_argument("--adj-nt", type=int, default=2000)
     ap.add_argument("--no-redfield", action="store_true",
                     help="skip the batched Redfield section")
+    ap.add_argument("--no-heom", action="store_true",
+                    help="skip the batched HEOM section")
     ap.add_argument("--no-large-n", action="store_true",
                     help="skip the single large-instance (GEMM schedule) section")
     ap.add_argument("--large-nt", type=int, default=100)
     ap.add_argument("--only-large-n", action="store_true",
                     help="run only the single large-instance (GEMM schedule) section")
+    ap.add_argument("--only-heom", action="store_true", help="run only the batched HEOM section")
+    ap.add_argument("--heom-n-inst", type=int, default=4096)
+    ap.add_argument("--heom-nt", type=int, default=1000)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -611,6 +693,13 @@ def main():
         from pyqed_gb300.build import build
         build()
         print(json.dumps(dict(large_n=measure_large_n(args, torch.device("cuda", 0)))))
+        return
+    if args.only_heom:
+        import torch
+        from pyqed_gb300.build import build
+        build()
+        print(json.dumps(dict(heom=measure_heom(args, torch.device("cuda", 0), n_inst=args.heom_n_inst,
+                                                nt=args.heom_nt))))
         return
     if args.only_adjoint:
         import torch

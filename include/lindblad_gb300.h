@@ -247,6 +247,59 @@ int lgb_redfield_propagate(lgb_redfield_t plan, const double* rho0, double* obs_
                            double* states_out, void* stream);
 int lgb_redfield_errors(lgb_redfield_t plan, int32_t* flags_host);
 
+/* ---- HEOM (hierarchical equations of motion) ----------------------------------
+ * Replaces HEOMSolver.run / propagator, _heom and _heom_propagator
+ * (pyqed/oqs.py:1332-1371, 1808-1935): one exponential bath mode coupled
+ * through one system operator sz, nado auxiliary density operators (the last
+ * one the zero terminator), explicit Euler steps swept level by level in place:
+ *     X_n += dt ( -i[H, X_n] - [sz, X_{n+1}] - n gamma X_n
+ *                 + n (Re D0 [sz, X_{n-1}] + i Im D0 {sz, X_{n-1}}) ),
+ * X_{n-1} already advanced in this step, X_{n+1} not yet. */
+typedef struct lgb_heom_plan* lgb_heom_t;
+
+enum {
+  LGB_HEOM_DOUBLE_FIRST = 1, /* advance level 0 twice per step (_heom_propagator)             */
+  LGB_HEOM_DIAG_SZ = 2       /* every sz is diagonal: its off-diagonal entries are not read */
+};
+
+typedef struct {
+  int32_t n_inst;       /* independent systems in the batch                          */
+  int32_t n_eops;       /* observables per system, <= 16                              */
+  int32_t nt;           /* Euler steps                                                */
+  int32_t nado;         /* levels per system including the zero terminator, >= 2     */
+  int32_t precision;    /* LGB_PREC_FP64 or LGB_PREC_FP32                             */
+  int32_t flags;        /* LGB_HEOM_DOUBLE_FIRST | LGB_HEOM_DIAG_SZ, or 0             */
+  double dt;
+} lgb_heom_problem_t;
+
+/* Largest supported system dimension (64). */
+int lgb_heom_max_dim(int32_t precision);
+/* Most levels whose hierarchy stays in shared memory at dimension n; deeper
+ * hierarchies run from a global workspace. */
+int lgb_heom_max_levels_on_chip(int32_t n, int32_t precision);
+
+int lgb_heom_create(lgb_heom_t* plan, const lgb_heom_problem_t* prob, const int32_t* dims);
+int lgb_heom_destroy(lgb_heom_t plan);
+/* info[4]: threads per system, systems per CTA, levels on chip (1/0), shared bytes per CTA. */
+int lgb_heom_layout(lgb_heom_t plan, int32_t* info);
+
+/* Device pointers, complex128 row-major, system b at offset sum_{c<b} N_c^2:
+ *   H, sz  the Hamiltonian and the system-bath operator
+ *   bath   n_inst x 3 FP64: gamma, Re D0, Im D0
+ *   eops   vec(O_e^T) per system, e-major (n_eops x N_b^2 at n_eops * offset) */
+int lgb_heom_set(lgb_heom_t plan, const double* H, const double* sz, const double* bath, const double* eops,
+                 void* stream);
+
+/* nt steps from X_0 = rho0 (packed), the other levels zero.
+ *   obs_out [n_inst][n_eops][nt] complex128, Tr[O X_0] after every step, or NULL
+ *   rho_out X_0 after nt steps (packed), or NULL
+ *   ado_out all nado levels after nt steps, system b at nado * offset
+ *           (level-major, the terminator written as zeros), or NULL
+ * A system whose X_0 becomes NaN/Inf stops with LGB_ERR_NONFINITE. */
+int lgb_heom_propagate(lgb_heom_t plan, const double* rho0, double* obs_out, double* rho_out, double* ado_out,
+                       void* stream);
+int lgb_heom_errors(lgb_heom_t plan, int32_t* flags_host);
+
 /* ---- propagation without device allocation ---------------------------------
  * No counterpart in the reference: pyqed is pure Python and never manages
  * device memory.

@@ -42,10 +42,14 @@ EXPORTS = [
     "lgb_propagate_noalloc", "lgb_plan_adjoint", "lgb_plan_set_option",
     "lgb_redfield_tensor", "lgb_redfield_max_dim", "lgb_redfield_create", "lgb_redfield_destroy",
     "lgb_redfield_set", "lgb_redfield_propagate", "lgb_redfield_errors",
+    "lgb_heom_max_dim", "lgb_heom_max_levels_on_chip", "lgb_heom_create", "lgb_heom_destroy",
+    "lgb_heom_layout", "lgb_heom_set", "lgb_heom_propagate", "lgb_heom_errors",
 ]
 # tuning options (lgb_option_t)
 OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3}
 FLAG_ADJOINT = 1
+HEOM_DOUBLE_FIRST = 1
+HEOM_DIAG_SZ = 2
 
 
 class LindbladError(RuntimeError):
@@ -78,6 +82,14 @@ class RedfieldProblem(ctypes.Structure):
     _fields_ = [
         ("n_inst", ctypes.c_int32), ("n_eops", ctypes.c_int32), ("nt", ctypes.c_int32),
         ("precision", ctypes.c_int32), ("store_every", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("dt", ctypes.c_double),
+    ]
+
+
+class HeomProblem(ctypes.Structure):
+    _fields_ = [
+        ("n_inst", ctypes.c_int32), ("n_eops", ctypes.c_int32), ("nt", ctypes.c_int32),
+        ("nado", ctypes.c_int32), ("precision", ctypes.c_int32), ("flags", ctypes.c_int32),
         ("dt", ctypes.c_double),
     ]
 
@@ -136,6 +148,22 @@ def lib():
     L.lgb_redfield_propagate.argtypes = [vp, dp, dp, dp, dp, vp]
     L.lgb_redfield_errors.restype = ctypes.c_int
     L.lgb_redfield_errors.argtypes = [vp, ctypes.POINTER(i32)]
+    L.lgb_heom_max_dim.restype = ctypes.c_int
+    L.lgb_heom_max_dim.argtypes = [i32]
+    L.lgb_heom_max_levels_on_chip.restype = ctypes.c_int
+    L.lgb_heom_max_levels_on_chip.argtypes = [i32, i32]
+    L.lgb_heom_create.restype = ctypes.c_int
+    L.lgb_heom_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(HeomProblem), ctypes.POINTER(i32)]
+    L.lgb_heom_destroy.restype = ctypes.c_int
+    L.lgb_heom_destroy.argtypes = [vp]
+    L.lgb_heom_layout.restype = ctypes.c_int
+    L.lgb_heom_layout.argtypes = [vp, ctypes.POINTER(i32)]
+    L.lgb_heom_set.restype = ctypes.c_int
+    L.lgb_heom_set.argtypes = [vp, dp, dp, dp, dp, vp]
+    L.lgb_heom_propagate.restype = ctypes.c_int
+    L.lgb_heom_propagate.argtypes = [vp, dp, dp, dp, dp, vp]
+    L.lgb_heom_errors.restype = ctypes.c_int
+    L.lgb_heom_errors.argtypes = [vp, ctypes.POINTER(i32)]
     L.lgb_plan_set_option.restype = ctypes.c_int
     L.lgb_plan_set_option.argtypes = [vp, i32, i32]
     L.lgb_plan_adjoint.restype = ctypes.c_int

@@ -113,3 +113,20 @@ def test_result_conventions(tmp_path):
     r.observables = np.zeros((11, 1))
     r.dump(str(tmp_path / "r.pkl"))
     assert load_result(str(tmp_path / "r.pkl")).nt == 10
+
+
+def test_heom_create_validates_before_any_device_call():
+    import ctypes
+    L = C.lib()
+    plan = ctypes.c_void_p()
+    dims = (ctypes.c_int32 * 1)(4)
+    for bad in (dict(nado=1), dict(n_eops=17), dict(flags=8), dict(nt=-1)):
+        kw = dict(n_inst=1, n_eops=0, nt=10, nado=4, precision=C.PREC["fp32"], flags=0, dt=0.01)
+        kw.update(bad)
+        prob = C.HeomProblem(**kw)
+        assert L.lgb_heom_create(ctypes.byref(plan), ctypes.byref(prob), dims) == C.LGB_ERR_INVALID_ARG
+    prob = C.HeomProblem(n_inst=1, n_eops=0, nt=10, nado=4, precision=C.PREC["3xtf32"], flags=0, dt=0.01)
+    assert L.lgb_heom_create(ctypes.byref(plan), ctypes.byref(prob), dims) == C.LGB_ERR_UNSUPPORTED
+    assert L.lgb_heom_max_dim(C.PREC["fp32"]) == 64
+    # N = 16: 200 KB of shared memory less the two operators, 4 KB per level
+    assert L.lgb_heom_max_levels_on_chip(16, C.PREC["fp64"]) == (200 * 1024 - 2 * 256 * 16) // 4096
