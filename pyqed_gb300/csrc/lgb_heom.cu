@@ -92,16 +92,16 @@ template <typename T2> __device__ __forceinline__ void cmsub(T2& c, const T2 a, 
 // share every column load): acc[e] = {Am X, X Am, sz Y, Y sz, sz Z, Z sz}
 // at (r_e, c), with Am = -iH, Y = X_{n+1} (old) and Z = X_{n-1} (new).  With
 // DIAG, S holds the diagonal of sz and its products are O(1) per element.
-template <typename T2, bool HY, bool HZ, bool DIAG>
-__device__ __forceinline__ void task_products(int N, int r0, int r1, int c, const T2* Am, const T2* S, const T2* X,
-                                              const T2* Y, const T2* Z, T2 (&acc)[2][6]) {
+template <typename T2, bool HY, bool HZ, bool DIAG, int NC>
+__device__ __forceinline__ void task_products(int n_rt, int r0, int r1, int c, const T2* Am, const T2* S,
+                                              const T2* X, const T2* Y, const T2* Z, T2 (&acc)[2][6]) {
+  const int N = NC > 0 ? NC : n_rt;  // NC > 0: the dimension is a compile-time constant
 #pragma unroll
   for (int e = 0; e < 2; ++e)
 #pragma unroll
     for (int q = 0; q < 6; ++q) acc[e][q] = mk<T2>(0.0, 0.0);
   const int R0 = r0 * N, R1 = r1 * N;
-#pragma unroll 2
-  for (int k = 0; k < N; ++k) {
+  auto kstep = [&](int k) {
     const int kc = k * N + c;
     const T2 xk = X[kc], ak = Am[kc];
     cmac(acc[0][0], Am[R0 + k], xk);
@@ -125,6 +125,13 @@ __device__ __forceinline__ void task_products(int N, int r0, int r1, int c, cons
         cmac(acc[1][5], Z[R1 + k], sk);
       }
     }
+  };
+  if constexpr (NC > 0) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) kstep(k);
+  } else {
+#pragma unroll 2
+    for (int k = 0; k < N; ++k) kstep(k);
   }
   if constexpr (DIAG && (HY || HZ)) {
     const T2 sc = S[c];
@@ -148,18 +155,18 @@ __device__ __forceinline__ void task_products(int N, int r0, int r1, int c, cons
 
 // f = Am X - X Am - sz Y + Y sz - ng X + cr (sz Z - Z sz) + i ci (sz Z + Z sz)
 // at (r0, c) and (r1, c).
-template <typename T2, bool DIAG>
+template <typename T2, bool DIAG, int NC>
 __device__ __forceinline__ void task_rhs(bool hy, bool hz, int N, int r0, int r1, int c, const T2* Am, const T2* S,
                                          const T2* X, const T2* Y, const T2* Z, decltype(T2{}.x) ng,
                                          decltype(T2{}.x) cr, decltype(T2{}.x) ci, T2& f0, T2& f1) {
   using T = decltype(T2{}.x);
   T2 acc[2][6];
   if (hy) {
-    if (hz) task_products<T2, true, true, DIAG>(N, r0, r1, c, Am, S, X, Y, Z, acc);
-    else task_products<T2, true, false, DIAG>(N, r0, r1, c, Am, S, X, Y, Z, acc);
+    if (hz) task_products<T2, true, true, DIAG, NC>(N, r0, r1, c, Am, S, X, Y, Z, acc);
+    else task_products<T2, true, false, DIAG, NC>(N, r0, r1, c, Am, S, X, Y, Z, acc);
   } else {
-    if (hz) task_products<T2, false, true, DIAG>(N, r0, r1, c, Am, S, X, Y, Z, acc);
-    else task_products<T2, false, false, DIAG>(N, r0, r1, c, Am, S, X, Y, Z, acc);
+    if (hz) task_products<T2, false, true, DIAG, NC>(N, r0, r1, c, Am, S, X, Y, Z, acc);
+    else task_products<T2, false, false, DIAG, NC>(N, r0, r1, c, Am, S, X, Y, Z, acc);
   }
   const T tng = ng, tcr = cr, tci = ci;
 #pragma unroll
@@ -182,11 +189,11 @@ __device__ __forceinline__ int ring(int x, int L) {
 // x + dt f; the FP32 path compensates level 0 (Kahan, in place: each element
 // of the compensation belongs to one thread)
 template <typename T2>
-__device__ __forceinline__ T2 euler_comp(T2 x, T2 f, double dt, T2* cp) {
+__device__ __forceinline__ T2 euler_comp(T2 x, T2 f, decltype(T2{}.x) dt, T2* cp) {
   using T = decltype(T2{}.x);
   if constexpr (sizeof(T) == 4) {
     const T2 c = *cp;
-    const T yx = (T)dt * f.x - c.x, yy = (T)dt * f.y - c.y;
+    const T yx = dt * f.x - c.x, yy = dt * f.y - c.y;
     const T tx = x.x + yx, ty = x.y + yy;
     *cp = make_float2((tx - x.x) - yx, (ty - x.y) - yy);
     return make_float2(tx, ty);
@@ -195,11 +202,10 @@ __device__ __forceinline__ T2 euler_comp(T2 x, T2 f, double dt, T2* cp) {
   }
 }
 template <typename T2>
-__device__ __forceinline__ T2 euler_plain(T2 x, T2 f, double dt) {
-  using T = decltype(T2{}.x);
+__device__ __forceinline__ T2 euler_plain(T2 x, T2 f, decltype(T2{}.x) dt) {
   T2 r;
-  r.x = x.x + f.x * (T)dt;
-  r.y = x.y + f.y * (T)dt;
+  r.x = x.x + f.x * dt;
+  r.y = x.y + f.y * dt;
   return r;
 }
 
@@ -211,7 +217,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
-template <typename T, bool ONCHIP, bool DIAG>
+template <typename T, bool ONCHIP, bool DIAG, int NC>
 __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2) heom_sweep_kernel(HeomParams p) {
   using T2 = typename Cplx<T>::type;
   constexpr bool KAHAN = sizeof(T) == 4;
@@ -223,7 +229,8 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
   if (b >= p.n_inst) return;  // no CTA-wide barrier below: each group syncs on its own id
   const int bid = 1 + g;
   const bool wg = G == 32;  // a one-warp group syncs with warp primitives
-  const int N = p.dims[b], M = N * N, L = p.nado, NS = p.NS;
+  // NC > 0: every system has dimension NC (compile-time loops and strides)
+  const int N = NC > 0 ? NC : p.dims[b], M = N * N, L = p.nado, NS = NC > 0 ? NC * NC : p.NS;
   const int h = (N + 1) >> 1, tasks = N * h;
   // levels (nado slots of NS) and, for FP32, the compensation of level 0
   const size_t lev_elems = (size_t)L * NS + (KAHAN ? NS : 0);
@@ -263,7 +270,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
   // level coefficients in the working precision (no FP64 arithmetic in the
   // FP32 sweep: GB300's FP64 pipe is narrow)
   const T tg = (T)p.bath[3 * b], tr = (T)p.bath[3 * b + 1], ti = (T)p.bath[3 * b + 2];
-  const double dt = p.dt;
+  const T dt = (T)p.dt;
   const int E = p.n_eops;
   const T2* Ot = reinterpret_cast<const T2*>(KAHAN ? (const void*)p.OtF : (const void*)p.Ot) + (long long)E * vo;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -284,7 +291,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
         const int rp = t / N, c = t - rp * N, r1 = rp + h;
         const bool two = r1 < N;
         T2 f0, f1;
-        task_rhs<T2, DIAG>(Y != nullptr, false, N, rp, two ? r1 : rp, c, Am, S, X, Y, nullptr, (T)0, (T)0, (T)0,
+        task_rhs<T2, DIAG, NC>(Y != nullptr, false, N, rp, two ? r1 : rp, c, Am, S, X, Y, nullptr, (T)0, (T)0, (T)0,
                            f0, f1);
         const int i0 = rp * N + c, i1 = r1 * N + c;
         Xs[i0] = euler_comp(X[i0], f0, dt, cmp + i0);
@@ -317,7 +324,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
         const int r1 = rp + h;
         const bool two = r1 < N;
         T2 f0, f1;
-        task_rhs<T2, DIAG>(hy, hz, N, rp, two ? r1 : rp, c, Am, S, X, Y, Z, ng, cr, ci, f0, f1);
+        task_rhs<T2, DIAG, NC>(hy, hz, N, rp, two ? r1 : rp, c, Am, S, X, Y, Z, ng, cr, ci, f0, f1);
         const int i0 = rp * N + c, i1 = r1 * N + c;
         if (n == 0) {
           const T2 v0 = euler_comp(X[i0], f0, dt, cmp + i0);
@@ -454,6 +461,7 @@ struct lgb_heom_plan {
   std::vector<long long> voff;
   long long tot_v = 0;
   int G = 32, gpc = 1, NS = 1;
+  int nconst = 0;  // the common dimension when it has a compiled sweep, else 0
   bool on_chip = true;
   size_t smem = 0;
   int* d_dims = nullptr;
@@ -480,6 +488,19 @@ void heom_free(lgb_heom_plan* pl) {
   cudaFree(pl->d_OtF);
   cudaFree(pl->d_ws);
   cudaFree(pl->d_err);
+}
+
+// the FP32 on-chip sweep with the dimension fixed at compile time (2, 4, 8,
+// 16) when every system of the batch has it, else the general kernel
+template <bool DIAG, typename F>
+cudaError_t heom_launch_fp32(int nconst, F&& launch) {
+  switch (nconst) {
+    case 2: return launch(lgb::heom_sweep_kernel<float, true, DIAG, 2>);
+    case 4: return launch(lgb::heom_sweep_kernel<float, true, DIAG, 4>);
+    case 8: return launch(lgb::heom_sweep_kernel<float, true, DIAG, 8>);
+    case 16: return launch(lgb::heom_sweep_kernel<float, true, DIAG, 16>);
+    default: return launch(lgb::heom_sweep_kernel<float, true, DIAG, 0>);
+  }
 }
 
 template <typename V>
@@ -540,6 +561,8 @@ int lgb_heom_create(lgb_heom_t* plan, const lgb_heom_problem_t* prob, const int3
     pl->tot_v += (long long)N * N;
   }
   pl->NS = nmax * nmax;
+  const bool uniform = std::all_of(pl->dims.begin(), pl->dims.end(), [&](int d) { return d == nmax; });
+  if (uniform && (nmax == 2 || nmax == 4 || nmax == 8 || nmax == 16)) pl->nconst = nmax;
   // one thread per (column, row pair) task
   const int tasks = nmax * ((nmax + 1) / 2);
   pl->G = std::min(lgb::kHThreads, std::max(32, (tasks + 31) / 32 * 32));
@@ -655,18 +678,18 @@ int lgb_heom_propagate(lgb_heom_t plan, const double* rho0, double* obs_out, dou
   const bool diag = (pr.flags & LGB_HEOM_DIAG_SZ) != 0;
   if (pr.precision == LGB_PREC_FP64) {
     if (diag)
-      e = plan->on_chip ? launch(lgb::heom_sweep_kernel<double, true, true>)
-                        : launch(lgb::heom_sweep_kernel<double, false, true>);
+      e = plan->on_chip ? launch(lgb::heom_sweep_kernel<double, true, true, 0>)
+                        : launch(lgb::heom_sweep_kernel<double, false, true, 0>);
     else
-      e = plan->on_chip ? launch(lgb::heom_sweep_kernel<double, true, false>)
-                        : launch(lgb::heom_sweep_kernel<double, false, false>);
+      e = plan->on_chip ? launch(lgb::heom_sweep_kernel<double, true, false, 0>)
+                        : launch(lgb::heom_sweep_kernel<double, false, false, 0>);
+  } else if (!plan->on_chip) {
+    e = diag ? launch(lgb::heom_sweep_kernel<float, false, true, 0>)
+             : launch(lgb::heom_sweep_kernel<float, false, false, 0>);
+  } else if (diag) {
+    e = heom_launch_fp32<true>(plan->nconst, launch);
   } else {
-    if (diag)
-      e = plan->on_chip ? launch(lgb::heom_sweep_kernel<float, true, true>)
-                        : launch(lgb::heom_sweep_kernel<float, false, true>);
-    else
-      e = plan->on_chip ? launch(lgb::heom_sweep_kernel<float, true, false>)
-                        : launch(lgb::heom_sweep_kernel<float, false, false>);
+    e = heom_launch_fp32<false>(plan->nconst, launch);
   }
   if (e != cudaSuccess) return LGB_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;

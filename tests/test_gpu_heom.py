@@ -179,3 +179,20 @@ def test_heom_ensemble_workload_fp32_vs_fp64():
         o = HO.heom_run(e["H"][b], e["rho0"][b], e["sz"][b], e["e_ops"][b], e["temperature"][b], e["cutoff"][b],
                         e["reorganization"][b], 8, 0.01, 400)
         assert np.abs(r64["observables"][b] - o).max() < 1e-10
+
+
+@pytest.mark.parametrize("N", [2, 4, 8, 16])
+@pytest.mark.parametrize("sz_kind", ["dense", "diag"])
+def test_heom_compiled_dimensions_vs_oracle(N, sz_kind):
+    """Batches of one dimension run the sweep compiled for it (N = 2, 4, 8, 16)."""
+    H, sz, rho0, e_ops, bath = _ragged_batch(40 + N, [N] * 11, 5)
+    if sz_kind == "diag":
+        rng = np.random.default_rng(41 + N)
+        sz = [np.diag(rng.standard_normal(N)).astype(complex) for _ in range(11)]
+    dt, nt = 0.01, 200
+    res = heom_batch(H, sz, rho0, e_ops, nado=5, dt=dt, nt=nt, bath=bath, precision="fp32", return_ado=True)
+    assert res["layout"]["sz"] == sz_kind
+    obs, ados = _oracle_batch(H, sz, rho0, e_ops, bath, 5, dt, nt)
+    for b in range(11):
+        assert np.abs(res["observables"][b] - obs[b]).max() < TOL["fp32"]
+        assert np.abs(res["ado"][b] - ados[b]).max() < TOL["fp32"]
