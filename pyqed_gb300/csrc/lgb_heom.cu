@@ -275,6 +275,21 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
   const T2* Ot = reinterpret_cast<const T2*>(KAHAN ? (const void*)p.OtF : (const void*)p.Ot) + (long long)E * vo;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w0 = (g * G) >> 5, nw = G >> 5;
+  // FP32 one-warp groups: widen the staged observables of steps [0, nsteps)
+  auto flush_obs = [&](int nsteps) {
+    if constexpr (KAHAN) {
+      if (wg && p.obs_out != nullptr) {
+        __syncwarp();
+        for (int e = 0; e < E; ++e) {
+          double2* row = p.obs_out + ((long long)b * E + e) * p.nt;
+          for (int st = lane; st < nsteps; st += 32) {
+            const float4 v = *reinterpret_cast<const float4*>(row + st);
+            row[st] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+          }
+        }
+      }
+    }
+  };
   // this thread's (row pair, column) task when every task fits the group (N <= 22)
   const bool one = tasks <= G;
   const int rp1 = gt / N, c1 = gt - rp1 * N;
@@ -379,6 +394,14 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
               ly += __shfl_xor_sync(0xffffffffu, ly, o) + er;
               hyv = s;
             }
+            if (wg) {
+              // staged as (hi, lo, hi, lo) in the 16-byte output slot and
+              // widened to FP64 by whole warps after the run (flush_obs)
+              if (lane == 0 && p.obs_out != nullptr)
+                *reinterpret_cast<float4*>(p.obs_out + ((long long)b * E + e) * p.nt + step) =
+                    make_float4(hx, lx, hyv, ly);
+              continue;
+            }
             sx = lane == 0 ? (double)hx + (double)lx : 0.0;
             sy = lane == 0 ? (double)hyv + (double)ly : 0.0;
           } else {
@@ -422,6 +445,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
         }
         if (bad) {
           if (gt == 0) p.err[b] = 4;  // LGB_ERR_NONFINITE
+          flush_obs(step + 1);
           return;
         }
       } else {
@@ -434,6 +458,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
     }
     kk = kk + 1 == L ? 0 : kk + 1;
   }
+  flush_obs(p.nt);
   // outputs: level n sits in slot (n - nt) mod L
   for (int l = 0; l < L; ++l) {
     const T2* X = lev + (size_t)ring(l - kk, L) * NS;

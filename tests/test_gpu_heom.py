@@ -154,18 +154,23 @@ def test_heom_layout_groups():
     assert lay["threads_per_system"] == 128 and lay["systems_per_cta"] == 2
 
 
-def test_heom_nonfinite_is_reported_per_system():
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_heom_nonfinite_is_reported_per_system(prec):
     H, sz, rho0, e_ops, bath = _ragged_batch(4, [3, 3, 3], 4)
     rho0[1] = rho0[1].copy()
     rho0[1][0, 0] = np.nan
     plans = []
-    res = heom_batch(H, sz, rho0, e_ops, nado=4, dt=0.01, nt=20, bath=bath, precision="fp64", _plan_out=plans)
+    res = heom_batch(H, sz, rho0, e_ops, nado=4, dt=0.01, nt=20, bath=bath, precision=prec, _plan_out=plans)
     with pytest.raises(C.LindbladError) as ei:
         plans[0].check_errors()
     assert ei.value.status == C.LGB_ERR_NONFINITE and "system 1" in str(ei.value)
     plans[0].close()
-    obs, _ = _oracle_batch([H[0]], [sz[0]], [rho0[0]], [e_ops[0]], [bath[0]], 4, 0.01, 20)
-    assert np.abs(res["observables"][0] - obs[0]).max() < 1e-10
+    obs, _ = _oracle_batch([H[0], H[2]], [sz[0], sz[2]], [rho0[0], rho0[2]], [e_ops[0], e_ops[2]],
+                           [bath[0], bath[2]], 4, 0.01, 20)
+    assert np.abs(res["observables"][0] - obs[0]).max() < TOL[prec]
+    assert np.abs(res["observables"][2] - obs[1]).max() < TOL[prec]
+    # the stopped system's first observable row (step 1) is already non-finite
+    assert not np.isfinite(res["observables"][1][:, 0]).all()
 
 
 def test_heom_ensemble_workload_fp32_vs_fp64():
