@@ -300,6 +300,25 @@ int lgb_heom_propagate(lgb_heom_t plan, const double* rho0, double* obs_out, dou
                        void* stream);
 int lgb_heom_errors(lgb_heom_t plan, int32_t* flags_host);
 
+/* ---- spectral (eigen-decomposition) evaluation ---------------------------------
+ * Replaces the mode sums of Lindblad_solver.evolve / correlation_2op_1t /
+ * correlation_2op_1w / correlation_3op_1t / correlation_3op_1w /
+ * correlation_3op_2t / correlation_4op_2t (pyqed/superoperator.py:455-770);
+ * the Liouvillian is diagonalised by the caller.  Device pointers, complex128
+ * interleaved, row-major; FP64 arithmetic; results are deterministic.
+ *
+ * lgb_spectral_sum: out[p][o] = sum_n W[o][n] f(lambda_n, x_p), p < n_x, o < n_out <= 16,
+ *   kind 0: f = exp(lambda x)          (time points)
+ *   kind 1: f = -1 / (lambda + i x)    (frequencies)
+ * x holds n_x real points (FP64). */
+int lgb_spectral_sum(int32_t k, int32_t n_out, int32_t n_x, int32_t kind, const double* lambda, const double* W,
+                     const double* x, double* out, void* stream);
+
+/* lgb_spectral_2t: cor[a][b] = sum_{m,n} exp(lambda_m tau_a) coeff[m][n] exp(lambda_n t_b),
+ * an n_tau x n_t matrix (the (len(taulist), len(tlist)) shape the reference returns). */
+int lgb_spectral_2t(int32_t k, int32_t n_tau, int32_t n_t, const double* lambda, const double* coeff,
+                    const double* tau, const double* t, double* cor, void* stream);
+
 /* ---- propagation without device allocation ---------------------------------
  * No counterpart in the reference: pyqed is pure Python and never manages
  * device memory.

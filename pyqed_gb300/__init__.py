@@ -10,8 +10,9 @@ from .oqs import LindbladSolver, liouvillian
 from .batch import propagate_batch, correlation_batch
 from .redfield import RedfieldSolver, redfield_batch
 from .heom import HEOMSolver, heom_batch
+from .spectral import Lindblad_solver
 from . import workloads
 
 __all__ = ["LindbladSolver", "Result", "load_result", "liouvillian", "propagate_batch",
-           "correlation_batch", "RedfieldSolver", "redfield_batch", "HEOMSolver", "heom_batch", "workloads"]
+           "correlation_batch", "RedfieldSolver", "redfield_batch", "HEOMSolver", "heom_batch", "Lindblad_solver", "workloads"]
 __version__ = "0.1.0"

@@ -44,6 +44,7 @@ EXPORTS = [
     "lgb_redfield_set", "lgb_redfield_propagate", "lgb_redfield_errors",
     "lgb_heom_max_dim", "lgb_heom_max_levels_on_chip", "lgb_heom_create", "lgb_heom_destroy",
     "lgb_heom_layout", "lgb_heom_set", "lgb_heom_propagate", "lgb_heom_errors",
+    "lgb_spectral_sum", "lgb_spectral_2t",
 ]
 # tuning options (lgb_option_t)
 OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3}
@@ -164,6 +165,10 @@ def lib():
     L.lgb_heom_propagate.argtypes = [vp, dp, dp, dp, dp, vp]
     L.lgb_heom_errors.restype = ctypes.c_int
     L.lgb_heom_errors.argtypes = [vp, ctypes.POINTER(i32)]
+    L.lgb_spectral_sum.restype = ctypes.c_int
+    L.lgb_spectral_sum.argtypes = [i32, i32, i32, i32, dp, dp, dp, dp, vp]
+    L.lgb_spectral_2t.restype = ctypes.c_int
+    L.lgb_spectral_2t.argtypes = [i32, i32, i32, dp, dp, dp, dp, dp, vp]
     L.lgb_plan_set_option.restype = ctypes.c_int
     L.lgb_plan_set_option.argtypes = [vp, i32, i32]
     L.lgb_plan_adjoint.restype = ctypes.c_int

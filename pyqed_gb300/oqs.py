@@ -36,15 +36,18 @@ def liouvillian(H, c_ops):
     ``pyqed.superoperator.liouvillian`` (``pyqed/superoperator.py:29-57``):
     -i (H x I - I x H^T) + sum_c [c x c* - 1/2 (c^dag c x I + I x (c^dag c)^T)].
     """
-    H = csr_matrix(to_dense(H))
+    # the same operations in the same order as the reference (dense c^dag c,
+    # each dissipator formed before it is added), so that L is bit-identical:
+    # the eigenvector phases of the spectral solver depend on its last bits
+    H = to_dense(H)
     N = H.shape[0]
-    idm = identity(N, format="csr")
+    idm = identity(N)
     L = -1j * (kron(H, idm) - kron(idm, H.T))
     for c in (c_ops or []):
-        c = csr_matrix(to_dense(c))
-        cdc = c.conj().T @ c
-        L = L + kron(c, c.conj()) - 0.5 * (kron(cdc, idm) + kron(idm, cdc.T))
-    return L.tocsr()
+        c = to_dense(c)
+        cdc = c.conjugate().transpose().dot(c)
+        L = L + (kron(c, c.conj()) - 0.5 * (kron(cdc, idm) + kron(idm, cdc.T)))
+    return csr_matrix(L)
 
 
 def _cops_for_engine(c_ops):

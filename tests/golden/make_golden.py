@@ -23,6 +23,9 @@ inputs) and the outputs of the reference's own entry points:
                      ``correlation_4op_1t`` (``pyqed/oqs.py:1193-1312``) on the
                      Jaynes-Cummings system, 50 steps.
 * ``redfield_*.npz`` ``RedfieldSolver.redfield_tensor`` / ``evolve``.
+* ``spectral_jc.npz`` the eigen-decomposition ``Lindblad_solver``
+                     (``pyqed/superoperator.py:455-770``) correlations on
+                     the Jaynes-Cummings system with 3 Fock states.
 * ``heom_*.npz``     ``HEOMSolver.run`` (``_heom``) on the reference's
                      spin-boson example and a 6-site chain, and
                      ``HEOMSolver.propagator`` (``_heom_propagator``) on a
@@ -126,6 +129,29 @@ def heom_fixtures(oqs):
     return out
 
 
+def spectral_fixtures():
+    import importlib
+    load()
+    so = importlib.import_module("pyqed.superoperator")
+    # 10. eigen-decomposition Lindblad solver (pyqed/superoperator.py:455-770)
+    # on the Jaynes-Cummings system with 3 Fock states (N = 6, 36 modes)
+    jc = W.jaynes_cummings(nfock=3)
+    H, c_ops, rho0 = jc["H"], jc["c_ops"], jc["rho0"]
+    a, b, c, d = jc["e_ops"][0], jc["c_ops"][0], jc["e_ops"][1], jc["c_ops"][1]
+    sol = so.Lindblad_solver(H, c_ops)
+    w, vr, vl = sol.eigenstates()
+    tl = np.linspace(0.0, 6.0, 13)
+    tau = np.linspace(0.0, 3.0, 5)
+    om = np.linspace(-2.1, 2.1, 8)
+    return {"spectral_jc": dict(
+        H=H, c_ops=np.stack(c_ops), rho0=rho0, ops=np.stack([a, b, c, d]), tlist=tl, taulist=tau, omegas=om,
+        eigvals=w, L=sol.L.toarray(),
+        c2_1t=sol.correlation_2op_1t(rho0, [a, b], tl), c2_1w=sol.correlation_2op_1w(rho0, [a, b], om),
+        c3_1t=sol.correlation_3op_1t(rho0, [a, b, c], tl), c3_1w=sol.correlation_3op_1w(rho0, [a, b, c], om),
+        c3_2t=sol.correlation_3op_2t(rho0, [a, b, c], tl, tau),
+        c4_2t=sol.correlation_4op_2t(rho0, [a, b, c, d], tl, tau))}
+
+
 def main():
     oqs = load()
     out = {}
@@ -223,6 +249,7 @@ def main():
 
     out.update(redfield_fixtures(oqs))
     out.update(heom_fixtures(oqs))
+    out.update(spectral_fixtures())
     save(out)
 
 
@@ -238,5 +265,7 @@ if __name__ == "__main__":
         save(redfield_fixtures(load()))
     elif sys.argv[1:] == ["heom"]:
         save(heom_fixtures(load()))
+    elif sys.argv[1:] == ["spectral"]:
+        save(spectral_fixtures())
     else:
         main()
