@@ -296,6 +296,8 @@ def run_gpu(args):
         line["redfield"] = measure_redfield(args, dev)
     if not args.no_heom:
         line["heom"] = measure_heom(args, dev, n_inst=args.heom_n_inst, nt=args.heom_nt)
+    if not args.no_spectral:
+        line["spectral"] = measure_spectral(args, dev)
     # CPU baseline (oracle port of the reference's dense algorithm) and accuracy
     if not args.no_cpu:
         line["cpu_baseline"], line["accuracy"] = cpu_baseline_and_accuracy(
@@ -544,6 +546,45 @@ def measure_heom(args, dev, n_inst=4096, n=8, nado=8, nt=1000, dt=0.01):
     return out
 
 
+def measure_spectral(args, dev, nfock=8, n_t=100000, n_tau=512):
+    """Eigen-decomposition solver on the Jaynes-Cummings system with 8 Fock
+    states (N = 16, 256 modes): correlation_2op_1t at 1e5 time points and the
+    two-time correlation_3op_2t on a 512 x 512 grid (GPU, CUDA events), the
+    host eigendecomposition, and numpy on the same mode sums."""
+    import torch
+    from pyqed_gb300 import workloads as W
+    from pyqed_gb300.spectral import Lindblad_solver
+    jc = W.jaynes_cummings(nfock=nfock)
+    H, c_ops, rho0 = jc["H"], jc["c_ops"], jc["rho0"]
+    a, b = jc["e_ops"][0], jc["e_ops"][1]
+    sol = Lindblad_solver(H, c_ops, device=dev)
+    t0 = time.perf_counter()
+    sol.eigenstates(complex_norm=True)
+    t_eig = time.perf_counter() - t0
+    tl = np.linspace(0.0, 200.0, n_t)
+    tau = np.linspace(0.0, 50.0, n_tau)
+    sol.correlation_2op_1t(rho0, [a, b], tl[:1000])
+    sol.correlation_3op_2t(rho0, [a, b, a], tau[:8], tau[:8])
+    out = dict(workload="jc%d spectral" % (2 * nfock), modes=int(sol.dim), n_t=n_t, n_tau=n_tau,
+               eig_seconds_host=t_eig)
+    for key, fn in (("corr_1t", lambda: sol.correlation_2op_1t(rho0, [a, b], tl)),
+                    ("corr_3op_2t", lambda: sol.correlation_3op_2t(rho0, [a, b, a], tau, tau))):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        out[key + "_seconds"] = time.perf_counter() - t1
+    if not args.no_cpu:
+        lam = sol.eigvals
+        co = sol._coeff_2op(rho0, a, b).cpu().numpy()
+        t1 = time.perf_counter()
+        _ = np.exp(np.outer(tl[:10000], lam)) @ co
+        out["corr_1t_numpy_seconds_10k_points"] = time.perf_counter() - t1
+    out["note"] = ("wall time per call incl. host mode weights and copies; the mode sums run in "
+                   "lgb_spectral_sum (FP64), the 2t grid as two ZGEMMs (lgb_spectral_2t)")
+    return out
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline / reference arm (the oracle port; the only oracle use here)
 # ---------------------------------------------------------------------------
@@ -676,6 +717,8 @@ def main():
                     help="skip the batched Redfield section")
     ap.add_argument("--no-heom", action="store_true",
                     help="skip the batched HEOM section")
+    ap.add_argument("--no-spectral", action="store_true",
+                    help="skip the eigen-decomposition (spectral) section")
     ap.add_argument("--no-large-n", action="store_true",
                     help="skip the single large-instance (GEMM schedule) section")
     ap.add_argument("--large-nt", type=int, default=100)
