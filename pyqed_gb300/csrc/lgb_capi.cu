@@ -143,14 +143,17 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   const bool split = prec == LGB_PREC_TF32X3 || prec == LGB_PREC_BF16X3;
   cudaDeviceGetAttribute(&pl->n_sm, cudaDevAttrMultiProcessorCount, pl->device);
 
-  // Tensor-core kernel: N <= 64 and no dense collapse operators (those keep
-  // the FP32 CTA kernel).  Its instances are padded to a multiple of 16.
+  // Tensor-core kernel: N <= 64 (padded to a multiple of 16), and N = 65 with
+  // a static H (a 64 x 64 block plus a SIMT border, padded to 68); no dense
+  // collapse operators (those keep the FP32 CTA kernel).
   std::vector<char> on_tc(n, 0);
   for (int b = 0; b < n; ++b)
-    on_tc[b] = split && !dense && pl->dims[b] <= lgb::tc_max_dim() && pr.schedule != LGB_SCHED_GEMM;
+    on_tc[b] = split && !dense && pr.schedule != LGB_SCHED_GEMM &&
+               (pl->dims[b] <= lgb::tc_max_dim() || (pl->dims[b] == lgb::tc_border_dim() && pr.n_drive == 0));
   for (int b = 0; b < n; ++b) {
     const long long N = pl->dims[b];
-    const int NP = on_tc[b] ? (int)((N + 15) / 16 * 16) : (int)((N + 3) / 4 * 4);
+    const int NP = !on_tc[b] ? (int)((N + 3) / 4 * 4)
+                             : (N > lgb::tc_max_dim() ? lgb::kTcBorderNpad : (int)((N + 15) / 16 * 16));
     pl->npad[b] = NP;
     pl->off[b] = pl->tot_off;
     pl->doff[b] = pl->tot_doff;

@@ -22,7 +22,12 @@ cudaError_t launch_cta_rk4(const CtaParams& p, int precision, int n_blocks, cuda
                            bool wide);
 
 // ---- tensor-core CTA-resident schedule (lgb_tc.cu) --------------------------
+// N <= tc_max_dim() runs as one padded block; N = tc_border_dim() with a static
+// H runs as a 64 x 64 block plus a SIMT border row and column, its working
+// matrices padded to kTcBorderNpad.
+constexpr int kTcBorderNpad = 68;
 int tc_max_dim();
+int tc_border_dim();
 int tc_smem_bytes(int precision, int npad);
 cudaError_t launch_tc_rk4(const CtaParams& p, int precision, const int* order, int n_items,
                           int* queue, int grid, cudaStream_t stream);

@@ -85,6 +85,29 @@ struct TcShared {
   float2 red[2][kMaxEops][kWarps];  // per-warp observable partials
 };
 
+// N = 65 (static H): the 64 x 64 block runs on the tensor cores as above; the
+// border row and column (index g = 64) run on the SIMT pipes while the MMAs
+// of the block are in flight.  With c_i = X[i][g], r_j = X[g][j], z = X[g][g],
+// a_i = A[i][g], b_j = A[g][j], alpha = A[g][g] and M the 64 x 64 block:
+//   block:   R_ij += a_i r_j + c_i conj(a_j)                       (epilogue)
+//   column:  R_ig = (A_M c)_i + a_i z + (M conj(b))_i + c_i conj(alpha) + D_ig c_i
+//   row:     R_gj = (b^T M)_j + alpha r_j + (conj(A_M) r)_j + z conj(a_j) + D_gj r_j
+//   corner:  R_gg = b.c + alpha z + r.conj(b) + z conj(alpha) + D_gg z
+// (M conj(b)) is reduced by the epilogue of the previous stage from its
+// registers; (b^T M) reads the X^T operand buffer; A_M c and conj(A_M) r read
+// A from global memory (L1/L2).  The border's RK4 state sits in shared memory
+// after the operand buffers.
+constexpr int kBorder = 65;  // border index 64 plus one (the corner is entry 64 of the row arrays)
+struct TcBorder {
+  float2 bx[2][2][kBorder];   // stage input [buffer][0: column c_i, 1: row r_j and corner]
+  float2 rho[2][kBorder], racc[2][kBorder], nkc[2][kBorder];
+  float2 aB[kBorder], bB[kBorder];      // A[i][g], A[g][j] (entry 64: alpha)
+  float2 dcol[kBorder], drow[kBorder];  // D[i][g], D[g][j]
+  float2 t1[64], t3[64], t4[64];        // (A_M c)_i, (b^T M)_j, (conj(A_M) r)_j of the stage
+  float2 t2p[2][64][4];                 // (M conj(b))_i partials of the four column groups, per bx buffer
+  float2 csum[2];                       // corner sums b.c and r.conj(b)
+};
+
 // Shared-memory geometry of one instance.  All operands are K-major with
 // core matrices of 8 rows x 16 bytes.
 //   "S" layout (A buffer, XM buffer): the K-direction core matrices of an
@@ -238,7 +261,7 @@ __device__ __forceinline__ void st4(unsigned char* base, const float* v) {
 // q = w & 3 and owns columns [(w >> 2) NP/4, (w >> 2 + 1) NP/4) of its lane;
 // lane l of the warp is TMEM lane 32 q + l = M row (c, i) with c = l >> 4,
 // i = 16 q + (l & 15); its partner (1 - c, i) is lane l ^ 16.
-template <bool BF16, int NP, int GR>
+template <bool BF16, int NP, int GR, bool BD = false>
 __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem, TcShared& sh,
                             const int grp, uint32_t& phase, bool& alive) {
   using El = Elem<BF16>;
@@ -258,7 +281,10 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const bool row_ok = i < NP;
   const int j0 = cg * NPQ;                   // first owned column
   const int N = p.dims[b];
-  const int NPS = NP + 2;                    // row stride of the FP32 working matrices
+  // padded dimension and row stride of the FP32 working matrices (NP, or 68
+  // for an instance with a border)
+  const int NPD = BD ? p.npad[b] : NP;
+  const int NPS = NPD + 2;
   const long long wo = p.woff[b];
   const int E = p.n_eops;
   const bool diag = p.cops_kind == 2 && p.n_cops > 0;
@@ -276,6 +302,8 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const uint32_t mshift = (uint32_t)grp * 8u * G::SBO_S;  // 64 rows
   const uint32_t tlane = tmem_d + ((uint32_t)(quarter * 32) << 16);
   uint64_t* mbar = &sh.mbar[grp];
+  TcBorder* bd = BD ? reinterpret_cast<TcBorder*>(smem + G::BYTES) : nullptr;
+  constexpr int kG = NP;  // border index (BD)
 
   // ---- A buffer: rows (0, r) = Ar[r], (1, r) = Ai[r]; hi level then lo level.
   // Rebuilt every step when driven.
@@ -287,7 +315,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
 #pragma unroll
         for (int d = 0; d < 4; ++d)
           if (d < p.n_drive) {
-            const float2 g = Gt[(long long)d * NP * NPS + k * NPS + r];
+            const float2 g = Gt[(long long)d * NPD * NPS + k * NPS + r];
             a.x = fmaf(f[d], g.x, a.x);
             a.y = fmaf(f[d], g.y, a.y);
           }
@@ -355,7 +383,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const bool use_mask = E * NPQ <= 32;
   if (use_mask && i < N) {
     for (int e = 0; e < E; ++e) {
-      const float2* o = OtF + (long long)e * NP * NPS + (long long)i * NPS + j0;
+      const float2* o = OtF + (long long)e * NPD * NPS + (long long)i * NPS + j0;
 #pragma unroll
       for (int jj = 0; jj < NPQ; ++jj) {
         const float2 ov = o[jj];
@@ -375,7 +403,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       float fx = 0.f, fy = 0.f;
       const uint32_t m = use_mask ? (omask >> (e * NPQ)) : 0xffffffffu;
       if (i < N && (m & ((NPQ >= 32) ? 0xffffffffu : ((1u << NPQ) - 1u))) != 0u) {
-        const float2* o = OtF + (long long)e * NP * NPS + (long long)i * NPS + j0;
+        const float2* o = OtF + (long long)e * NPD * NPS + (long long)i * NPS + j0;
         float2 ov[NPQ];
         // all loads issued before the first FMA (independent, predicated)
 #pragma unroll
@@ -392,12 +420,30 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
           }
         }
       }
+      if constexpr (BD) {
+        // border element (t, g) for t < 64, (g, t - 64) otherwise: O^T entry
+        // [i][j] = O[j][i] at i * NPS + j
+        if (tid < 2 * kG + 1) {
+          const bool col = tid < kG;
+          const int t = col ? tid : tid - kG;
+          const float2 ov = OtF[(long long)e * NPD * NPS + (col ? t * NPS + kG : kG * NPS + t)];
+          const float2 rv = bd->rho[col ? 0 : 1][t];
+          fx = fmaf(ov.x, rv.x, fmaf(-ov.y, rv.y, fx));
+          fy = fmaf(ov.x, rv.y, fmaf(ov.y, rv.x, fy));
+        }
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         fx += __shfl_xor_sync(0xffffffffu, fx, o);
         fy += __shfl_xor_sync(0xffffffffu, fy, o);
       }
       if (lane == 0) sh.red[grp][e][warp] = make_float2(fx, fy);
+    }
+    if constexpr (BD) {
+      if (tid < 2 * kG + 1) {
+        const float2 rv = bd->rho[tid < kG ? 0 : 1][tid < kG ? tid : tid - kG];
+        fin = fin && isfinite(rv.x) && isfinite(rv.y);
+      }
     }
     return fin;
   };
@@ -487,6 +533,165 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     const float x4[4] = {rho2[2 * g].x, rho2[2 * g].y, rho2[2 * g + 1].x, rho2[2 * g + 1].y};
     write_group(g, x4);
   }
+  // ---- border (BD): constants, state, and the (M conj(b)) partials of rho0
+  int bcur = 0;  // border buffer holding the current stage input
+  if constexpr (BD) {
+    const double2* r0 = p.rho0 + p.off[b];
+    for (int t = tid; t < kBorder; t += kT) {
+      bd->aB[t] = At0[kG * NPS + t];  // A[t][g]
+      bd->bB[t] = At0[t * NPS + kG];  // A[g][t]
+      bd->dcol[t] = diag ? Dm[t * NPS + kG] : make_float2(0.f, 0.f);
+      bd->drow[t] = diag ? Dm[kG * NPS + t] : make_float2(0.f, 0.f);
+    }
+    if (tid < 2 * kG + 1) {  // thread t owns border element (t, g) or (g, t - 64)
+      const bool col = tid < kG;
+      const int t = col ? tid : tid - kG, sl = col ? 0 : 1;
+      const double2 z = col ? r0[(long long)t * N + kG] : r0[(long long)kG * N + t];
+      const float2 v = make_float2((float)z.x, (float)z.y);
+      bd->rho[sl][t] = v;
+      bd->bx[0][sl][t] = v;
+      bd->racc[sl][t] = make_float2(0.f, 0.f);
+      bd->nkc[sl][t] = make_float2(0.f, 0.f);
+    }
+    gsync<GR>(grp);
+    float tx = 0.f, ty = 0.f;
+#pragma unroll
+    for (int jj = 0; jj < NPQ; ++jj) {
+      const float2 bj = bd->bB[j0 + jj];
+      const float v = rho_at(jj);  // c = 0: Re M_ij, c = 1: Im M_ij
+      tx = fmaf(v, c == 0 ? bj.x : bj.y, tx);
+      ty = fmaf(v, c == 0 ? -bj.y : bj.x, ty);
+    }
+    tx += __shfl_xor_sync(0xffffffffu, tx, 16);
+    ty += __shfl_xor_sync(0xffffffffu, ty, 16);
+    if (c == 0) bd->t2p[0][i][cg] = make_float2(tx, ty);
+  }
+  // Border work of one stage, run while the block's MMAs are in flight: the
+  // mode sums, then (after a barrier) the RK4 update of the 129 border
+  // elements into the other border buffer.
+  auto border_phase = [&](int stage) {
+    if constexpr (BD) {
+      const float2* bc = bd->bx[bcur][0];
+      const float2* br = bd->bx[bcur][1];
+      {  // (A_M c)_i and (conj(A_M) r)_j: four threads per row, 16 k each
+        const int d = tid >> 2, q = tid & 3;
+        const int row = d & (kG - 1);
+        const bool t4 = d >= kG;
+        float sx = 0.f, sy = 0.f;
+#pragma unroll 4
+        for (int kk = 0; kk < 16; ++kk) {
+          const int k = q * 16 + kk;
+          const float2 a = At0[k * NPS + row];  // A[row][k]
+          const float2 v = t4 ? br[k] : bc[k];
+          const float ay = t4 ? -a.y : a.y;
+          sx = fmaf(a.x, v.x, fmaf(-ay, v.y, sx));
+          sy = fmaf(a.x, v.y, fmaf(ay, v.x, sy));
+        }
+        sx += __shfl_xor_sync(0xffffffffu, sx, 1);
+        sy += __shfl_xor_sync(0xffffffffu, sy, 1);
+        sx += __shfl_xor_sync(0xffffffffu, sx, 2);
+        sy += __shfl_xor_sync(0xffffffffu, sy, 2);
+        if (q == 0) (t4 ? bd->t4 : bd->t1)[row] = make_float2(sx, sy);
+      }
+      {  // (b^T M)_j from the X^T operand (hi + lo): eight threads per column, 8 k each
+        const int j = tid >> 3, q = tid & 7;
+        const int rr = ncol(0, j), ri = ncol(1, j);
+        float sx = 0.f, sy = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+          const int k = q * 8 + kk;
+          const uint32_t o_r = off_t<BF16, NP>(rr, k), o_i = off_t<BF16, NP>(ri, k);
+          const float mr = (float)*reinterpret_cast<const ET*>(SXT + o_r) +
+                           (float)*reinterpret_cast<const ET*>(SXT + G::LVL_T + o_r);
+          const float mi = (float)*reinterpret_cast<const ET*>(SXT + o_i) +
+                           (float)*reinterpret_cast<const ET*>(SXT + G::LVL_T + o_i);
+          const float2 bk = bd->bB[k];
+          sx = fmaf(bk.x, mr, fmaf(-bk.y, mi, sx));
+          sy = fmaf(bk.x, mi, fmaf(bk.y, mr, sy));
+        }
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+          sx += __shfl_xor_sync(0xffffffffu, sx, o);
+          sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        }
+        if (q == 0) bd->t3[j] = make_float2(sx, sy);
+      }
+      if (warp == kW - 1) {  // corner sums b.c and r.conj(b)
+        float ux = 0.f, uy = 0.f, vx = 0.f, vy = 0.f;
+        for (int k = lane; k < kG; k += 32) {
+          const float2 bk = bd->bB[k], ck = bc[k], rk = br[k];
+          ux = fmaf(bk.x, ck.x, fmaf(-bk.y, ck.y, ux));
+          uy = fmaf(bk.x, ck.y, fmaf(bk.y, ck.x, uy));
+          vx = fmaf(rk.x, bk.x, fmaf(rk.y, bk.y, vx));
+          vy = fmaf(rk.y, bk.x, fmaf(-rk.x, bk.y, vy));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          ux += __shfl_xor_sync(0xffffffffu, ux, o);
+          uy += __shfl_xor_sync(0xffffffffu, uy, o);
+          vx += __shfl_xor_sync(0xffffffffu, vx, o);
+          vy += __shfl_xor_sync(0xffffffffu, vy, o);
+        }
+        if (lane == 0) {
+          bd->csum[0] = make_float2(ux, uy);
+          bd->csum[1] = make_float2(vx, vy);
+        }
+      }
+      gsync<GR>(grp);
+      if (tid < 2 * kG + 1) {
+        const bool col = tid < kG;
+        const int t = col ? tid : tid - kG, sl = col ? 0 : 1;
+        const float2 z = br[kG], al = bd->aB[kG];
+        const float2 alc = make_float2(al.x, -al.y);
+        float2 R;
+        if (col) {
+          const float2 x = bc[t], a = bd->aB[t];
+          const float2* tp = bd->t2p[bcur][t];
+          R = bd->t1[t];
+          R.x += (tp[0].x + tp[1].x) + (tp[2].x + tp[3].x);
+          R.y += (tp[0].y + tp[1].y) + (tp[2].y + tp[3].y);
+          cmac(R, a, z);
+          cmac(R, x, alc);
+          cmac(R, bd->dcol[t], x);
+        } else if (t < kG) {
+          const float2 x = br[t], a = bd->aB[t];
+          R = bd->t3[t];
+          R.x += bd->t4[t].x;
+          R.y += bd->t4[t].y;
+          cmac(R, al, x);
+          cmac(R, z, make_float2(a.x, -a.y));
+          cmac(R, bd->drow[t], x);
+        } else {
+          R = bd->csum[0];
+          R.x += bd->csum[1].x;
+          R.y += bd->csum[1].y;
+          cmac(R, al, z);
+          cmac(R, z, alc);
+          cmac(R, bd->drow[kG], z);
+        }
+        const float2 rh = bd->rho[sl][t];
+        float2 xn;
+        if (stage == 0) {
+          bd->racc[sl][t] = R;
+          xn = make_float2(fmaf(half_dt, R.x, rh.x), fmaf(half_dt, R.y, rh.y));
+        } else if (stage < 3) {
+          const float2 ra = bd->racc[sl][t];
+          bd->racc[sl][t] = make_float2(fmaf(2.f, R.x, ra.x), fmaf(2.f, R.y, ra.y));
+          const float h = stage == 2 ? dt : half_dt;
+          xn = make_float2(fmaf(h, R.x, rh.x), fmaf(h, R.y, rh.y));
+        } else {
+          // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4), as the block
+          const float2 ra = bd->racc[sl][t], nk = bd->nkc[sl][t];
+          const float yx = fmaf(sixth_dt, ra.x + R.x, nk.x), yy = fmaf(sixth_dt, ra.y + R.y, nk.y);
+          const float tx = rh.x + yx, ty = rh.y + yy;
+          bd->nkc[sl][t] = make_float2(yx - (tx - rh.x), yy - (ty - rh.y));
+          xn = make_float2(tx, ty);
+          bd->rho[sl][t] = xn;
+        }
+        bd->bx[bcur ^ 1][sl][t] = xn;
+      }
+    }
+  };
   if (tid == 0) p.err[b] = 0;
   if (p.obs_t0) obs_finish(obs_partials(), 0);
   // The observables of step s are reduced while the MMAs of the first stage
@@ -514,6 +719,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         issue_stage<BF16, NP>(tmem_d, sbase, mshift);
         mma_commit(mbar);
       }
+      border_phase(stage);
       if (stage == 0 && pend_row >= 0) pend_fin = obs_partials();
       if (!wait_mma()) break;
       if (stage == 0 && pend_row >= 0) {
@@ -541,6 +747,19 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         const float sg = c == 0 ? -1.f : 1.f;
         const float2 sg2 = make_float2(sg, sg), m1 = make_float2(-1.f, -1.f);
         const float ddxd = dd * xd;
+        // BD: this thread's component of a_i r_j + c_i conj(a_j) is
+        // u0 r_j.x + u1 r_j.y + u2 a_j.x + u3 a_j.y; tx, ty accumulate the
+        // (M conj(b))_i partial of the next stage input
+        [[maybe_unused]] float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f, tx = 0.f, ty = 0.f;
+        [[maybe_unused]] const float2* brow = nullptr;
+        if constexpr (BD) {
+          const float2 ai = bd->aB[i], ci = bd->bx[bcur][0][i];
+          u0 = c == 0 ? ai.x : ai.y;
+          u1 = c == 0 ? -ai.y : ai.x;
+          u2 = c == 0 ? ci.x : ci.y;
+          u3 = c == 0 ? ci.y : -ci.x;
+          brow = bd->bx[bcur][1];
+        }
 #pragma unroll
         for (int g = 0; g < NG; ++g) {
           const int col = j0 + g * 4;
@@ -574,6 +793,12 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
                 if (u) R.y = r; else R.x = r;
               }
             }
+            if constexpr (BD) {
+              const int j = col + 2 * h;
+              const float2 r0 = brow[j], r1 = brow[j + 1], a0 = bd->aB[j], a1 = bd->aB[j + 1];
+              R.x = fmaf(u0, r0.x, fmaf(u1, r0.y, fmaf(u2, a0.x, fmaf(u3, a0.y, R.x))));
+              R.y = fmaf(u0, r1.x, fmaf(u1, r1.y, fmaf(u2, a1.x, fmaf(u3, a1.y, R.y))));
+            }
             if constexpr (STAGE == 0) {
               racc2[k] = R;
               xn2[h] = __ffma2_rn(cst2, R, rho2[k]);
@@ -592,9 +817,22 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
               xd = (2 * k == dpos) ? xn2[h].x : xd;
               xd = (2 * k + 1 == dpos) ? xn2[h].y : xd;
             }
+            if constexpr (BD) {
+              const int j = col + 2 * h;
+              const float2 b0 = bd->bB[j], b1 = bd->bB[j + 1];
+              tx = fmaf(xn2[h].x, c == 0 ? b0.x : b0.y, tx);
+              ty = fmaf(xn2[h].x, c == 0 ? -b0.y : b0.x, ty);
+              tx = fmaf(xn2[h].y, c == 0 ? b1.x : b1.y, tx);
+              ty = fmaf(xn2[h].y, c == 0 ? -b1.y : b1.x, ty);
+            }
           }
           const float x4[4] = {xn2[0].x, xn2[0].y, xn2[1].x, xn2[1].y};
           write_group(g, x4);
+        }
+        if constexpr (BD) {
+          tx += __shfl_xor_sync(0xffffffffu, tx, 16);
+          ty += __shfl_xor_sync(0xffffffffu, ty, 16);
+          if (c == 0) bd->t2p[bcur ^ 1][i][cg] = make_float2(tx, ty);
         }
       };
       using S0 = std::integral_constant<int, 0>;
@@ -609,6 +847,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       if (stage == 0) by_mode(S0{});
       else if (stage < 3) by_mode(S1{});
       else by_mode(S3{});
+      bcur ^= 1;
     }
     if (!alive || nonfinite) break;
     pend_row = step + p.obs_t0;
@@ -621,6 +860,14 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         const int j = j0 + jj;
         if (j < N) reinterpret_cast<double*>(dst + (long long)i * N + j)[c] = (double)rho_at(jj);
       }
+      if constexpr (BD) {
+        if (tid < 2 * kG + 1) {
+          const bool col = tid < kG;
+          const int t = col ? tid : tid - kG;
+          const float2 v = bd->rho[col ? 0 : 1][t];
+          dst[col ? (long long)t * N + kG : (long long)kG * N + t] = make_double2(v.x, v.y);
+        }
+      }
     }
   }
 
@@ -632,6 +879,14 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     for (int jj = 0; jj < NPQ; ++jj) {
       const int j = j0 + jj;
       if (j < N) reinterpret_cast<double*>(dst + (long long)i * N + j)[c] = (double)rho_at(jj);
+    }
+    if constexpr (BD) {
+      if (tid < 2 * kG + 1) {
+        const bool col = tid < kG;
+        const int t = col ? tid : tid - kG;
+        const float2 v = bd->rho[col ? 0 : 1][t];
+        dst[col ? (long long)t * N + kG : (long long)kG * N + t] = make_double2(v.x, v.y);
+      }
     }
   }
   // TMEM reads of this instance are done before the next instance's first MMA
@@ -687,6 +942,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
       case 16: tc_instance<BF16, 16, 1>(p, b, smem, sh, 0, phase, alive); break;
       case 32: tc_instance<BF16, 32, 1>(p, b, smem, sh, 0, phase, alive); break;
       case 48: tc_instance<BF16, 48, 1>(p, b, smem, sh, 0, phase, alive); break;
+      case kTcBorderNpad: tc_instance<BF16, 64, 1, true>(p, b, smem, sh, 0, phase, alive); break;
       default: tc_instance<BF16, 64, 1>(p, b, smem, sh, 0, phase, alive); break;
     }
   }
@@ -731,6 +987,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
 }  // namespace
 
 int tc_max_dim() { return 64; }
+int tc_border_dim() { return 65; }
 
 int tc_smem_bytes(int precision, int npad) {
   const bool bf16 = precision == LGB_PREC_BF16X3;
@@ -740,6 +997,9 @@ int tc_smem_bytes(int precision, int npad) {
     case 16:
     case 32: return dual;
     case 48: return std::max(dual, bf16 ? (int)Geo<true, 48>::BYTES : (int)Geo<false, 48>::BYTES);
+    case kTcBorderNpad:
+      return std::max(dual, (bf16 ? (int)Geo<true, 64>::BYTES : (int)Geo<false, 64>::BYTES) +
+                                (int)sizeof(TcBorder));
     default: return std::max(dual, bf16 ? (int)Geo<true, 64>::BYTES : (int)Geo<false, 64>::BYTES);
   }
 }

@@ -227,6 +227,56 @@ def test_split_complex_dissipator_and_states():
             assert np.abs(res["states"][b][k] - states[2 * k + 1]).max() < TOL32
 
 
+@pytest.mark.parametrize("prec,tol", [("3xtf32", TOL32), ("3xbf16", TOLBF)])
+@pytest.mark.parametrize("kind", ["dephasing", "complex"])
+def test_split_border_n65_vs_oracle(prec, tol, kind):
+    """N = 65 runs on the tensor cores as a 64 x 64 block plus a SIMT border
+    row and column: dense GUE H (every border coupling non-zero), diagonal
+    collapse operators (pure dephasing, or complex with off-diagonal D),
+    observables with a t0 row and stored states, beside N = 64 and N = 16."""
+    rng = np.random.default_rng(31)
+    dims = [65, 64, 65, 16]
+    H, cops, rho0, eops = [], [], [], []
+    for N in dims:
+        H.append(W.gue_matrix(rng, N))
+        if kind == "dephasing":
+            cops.append([np.diag(np.sqrt(0.05) * (np.arange(N) == k)).astype(complex) for k in range(0, N, 7)])
+        else:
+            cops.append([np.diag((rng.standard_normal(N) + 1j * rng.standard_normal(N)) * 0.1) for _ in range(2)])
+        r = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+        rho0.append(r / np.linalg.norm(r))
+        eops.append([H[-1], W.gue_matrix(rng, N)])
+    nt, dt = 16, 0.02
+    res = propagate_batch(H, cops, rho0, dt, nt, e_ops=eops, obs_t0=True, store_every=4, precision=prec)
+    for b, N in enumerate(dims):
+        obs, states = O.lindblad(H[b], rho0[b], cops[b], eops[b], Nt=nt, dt=dt)
+        assert np.abs(res["rho"][b] - states[-1]).max() < tol, (b, N)
+        assert np.abs(res["observables"][b] - obs).max() < tol * N, (b, N)
+        for k in range(nt // 4):
+            assert np.abs(res["states"][b][k] - states[4 * k + 3]).max() < tol, (b, N, k)
+
+
+def test_split_border_driven_n65_takes_the_fp32_kernel():
+    """A driven N = 65 instance keeps the FP32 wide kernel beside tensor-core ones."""
+    rng = np.random.default_rng(32)
+    dims = [65, 40]
+    E = W.gp_pulse(12, 0.02, seed=3, amp=0.3)
+    H0 = [W.gue_matrix(rng, N) for N in dims]
+    mu = [W.gue_matrix(rng, N) for N in dims]
+    cops = [[np.diag(np.sqrt(0.02) * (np.arange(N) == k)) for k in range(3)] for N in dims]
+    rho0 = []
+    for N in dims:
+        psi = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        psi /= np.linalg.norm(psi)
+        rho0.append(np.outer(psi, psi.conj()))
+    res = propagate_batch(H0, cops, rho0, 0.02, 12, e_ops=[[m] for m in mu], obs_t0=False,
+                          precision="3xtf32", drive_ops=[[m] for m in mu], drive=E[None, :])
+    for b in range(len(dims)):
+        obs, states = O.lindblad_driven([H0[b], [mu[b], E]], rho0[b], cops[b], [mu[b]], Nt=12, dt=0.02)
+        assert np.abs(res["rho"][b] - states[-1]).max() < TOL32
+        assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < TOL32 * 10
+
+
 def test_split_driven_diag_vs_oracle():
     rng = np.random.default_rng(22)
     dims = [8, 33, 64]
