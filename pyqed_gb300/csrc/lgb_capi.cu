@@ -46,7 +46,7 @@ void free_plan(lgb_plan* pl) {
   pl->blas = nullptr;
   for (void* p : pl->allocations) cudaFree(p);
   pl->allocations.clear();
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < 3; ++k) {
     if (pl->side[k]) cudaStreamDestroy(pl->side[k]);
     if (pl->ev_join[k]) cudaEventDestroy(pl->ev_join[k]);
     pl->side[k] = nullptr;
@@ -175,7 +175,7 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   std::vector<char> wide(n, 0);
   for (int b = 0; b < n && cta_ok; ++b) {
     if (on_tc[b]) {
-      tc_maxnp = std::max(tc_maxnp, pl->npad[b]);
+      if (pl->npad[b] != lgb::kTcBorderNpad) tc_maxnp = std::max(tc_maxnp, pl->npad[b]);
       continue;
     }
     if (pl->npad[b] > lgb::cta_max_npad()) {
@@ -209,6 +209,7 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
     }
   }
   if (tc_maxnp > 0) tc_smem = lgb::tc_smem_bytes(prec, tc_maxnp);
+  pl->tcb_smem = lgb::tc_smem_bytes(prec, lgb::kTcBorderNpad);
   if (sched == LGB_SCHED_AUTO) sched = cta_ok ? LGB_SCHED_CTA : LGB_SCHED_GEMM;
   if (sched == LGB_SCHED_CTA && !cta_ok) {
     delete pl;
@@ -222,7 +223,9 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   // Largest instances first: with one CTA per instance the hardware block
   // scheduler then performs longest-processing-time-first list scheduling;
   // the tensor-core kernel's work queue hands them out in the same order.
-  for (int b = 0; b < n; ++b) (on_tc[b] ? pl->tc_order : (wide[b] ? pl->order_w : pl->order)).push_back(b);
+  for (int b = 0; b < n; ++b)
+    (on_tc[b] ? (pl->npad[b] == lgb::kTcBorderNpad ? pl->tcb_order : pl->tc_order)
+              : (wide[b] ? pl->order_w : pl->order)).push_back(b);
   auto by_size = [&](int a, int c) { return pl->dims[a] > pl->dims[c]; };
   std::stable_sort(pl->order.begin(), pl->order.end(), by_size);
   std::stable_sort(pl->order_w.begin(), pl->order_w.end(), by_size);
@@ -232,9 +235,10 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
     pl->order.clear();
     pl->order_w.clear();
     pl->tc_order.clear();
+    pl->tcb_order.clear();
   }
   const int n_launch = (pl->order.empty() ? 0 : 1) + (pl->order_w.empty() ? 0 : 1) +
-                       (pl->tc_order.empty() ? 0 : 1);
+                       (pl->tc_order.empty() ? 0 : 1) + (pl->tcb_order.empty() ? 0 : 1);
   bool ok = cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) == cudaSuccess;
   for (int k = 0; k + 1 < n_launch && ok; ++k) {
     ok = cudaStreamCreateWithFlags(&pl->side[k], cudaStreamNonBlocking) == cudaSuccess &&
@@ -254,6 +258,7 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   s = s ? s : upload(pl, &pl->d_order, pl->order);
   s = s ? s : upload(pl, &pl->d_order_w, pl->order_w);
   s = s ? s : upload(pl, &pl->d_tc_order, pl->tc_order);
+  s = s ? s : upload(pl, &pl->d_tcb_order, pl->tcb_order);
   s = s ? s : dalloc(pl, &pl->d_queue, sizeof(int));
   s = s ? s : upload(pl, &pl->d_off, pl->off);
   s = s ? s : upload(pl, &pl->d_doff, pl->doff);
@@ -521,18 +526,19 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
     }
     return LGB_OK;
   }
-  // Up to three kernels (wide FP32 CTA, FP32 CTA, tensor-core) cover the
-  // batch; the first runs on the caller's stream, the others on forked
-  // streams joined back before return.
+  // Up to four kernels (tensor-core border, wide FP32 CTA, FP32 CTA,
+  // tensor-core) cover the batch; the first runs on the caller's stream, the
+  // others on forked streams joined back before return.
   struct Launch {
-    int kind;  // 0 tensor core, 1 CTA, 2 wide CTA
+    int kind;  // 0 tensor core, 1 CTA, 2 wide CTA, 3 tensor-core border
     int count;
   };
-  Launch ls[3];
+  Launch ls[4];
   int nl = 0;
-  // The per-instance CTA kernels hold the longest single instances; they are
+  // The per-instance kernels hold the longest single instances; they are
   // launched first so that their blocks are resident from the start, and the
   // persistent tensor-core blocks fill the remaining SMs from the work queue.
+  if (!plan->tcb_order.empty()) ls[nl++] = {3, (int)plan->tcb_order.size()};
   if (!plan->order_w.empty()) ls[nl++] = {2, (int)plan->order_w.size()};
   if (!plan->order.empty()) ls[nl++] = {1, (int)plan->order.size()};
   if (!plan->tc_order.empty()) ls[nl++] = {0, (int)plan->tc_order.size()};
@@ -549,6 +555,9 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
       p.smem_bytes = plan->tc_smem;
       e = lgb::launch_tc_rk4(p, pr.precision, plan->d_tc_order, ls[k].count, plan->d_queue,
                              std::min(plan->n_sm, ls[k].count), s_k);
+    } else if (ls[k].kind == 3) {
+      p.smem_bytes = plan->tcb_smem;
+      e = lgb::launch_tc_border(p, pr.precision, plan->d_tcb_order, ls[k].count, s_k);
     } else {
       p.order = ls[k].kind == 1 ? plan->d_order : plan->d_order_w;
       p.smem_bytes = ls[k].kind == 1 ? plan->smem_bytes : plan->smem_w;
@@ -697,9 +706,10 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
   if (plan == nullptr || info == nullptr) return LGB_ERR_INVALID_ARG;
   info->schedule = plan->schedule;
   info->precision = plan->prob.precision;
-  info->smem_bytes = std::max(std::max(plan->smem_bytes, plan->smem_w), plan->tc_smem);
+  info->smem_bytes = std::max(std::max(plan->smem_bytes, plan->smem_w),
+                              plan->tcb_order.empty() ? plan->tc_smem : std::max(plan->tc_smem, plan->tcb_smem));
   info->launches_per_propagate = (plan->order.empty() ? 0 : 1) + (plan->order_w.empty() ? 0 : 1) +
-                                 (plan->tc_order.empty() ? 0 : 1);
+                                 (plan->tc_order.empty() ? 0 : 1) + (plan->tcb_order.empty() ? 0 : 1);
   if (plan->schedule == LGB_SCHED_GEMM) {
     // per instance: init (+ t0 observables) + per step (drive) + 4 x (G1, G2, epilogue);
     // split precision: init also converts X (2 kernels), the drive step also

@@ -31,6 +31,8 @@ int tc_border_dim();
 int tc_smem_bytes(int precision, int npad);
 cudaError_t launch_tc_rk4(const CtaParams& p, int precision, const int* order, int n_items,
                           int* queue, int grid, cudaStream_t stream);
+cudaError_t launch_tc_border(const CtaParams& p, int precision, const int* order, int n_items,
+                             cudaStream_t stream);
 
 // ---- discrete adjoint (lgb_adjoint.cu) ------------------------------------------
 struct AdjParams {
@@ -194,7 +196,9 @@ struct lgb_plan {
   std::vector<int> dims, npad, order;      // order: CTA-kernel instances, largest first
   std::vector<int> order_w;                // 384-thread FP32 CTA-kernel instances (64 < N <= 76)
   std::vector<int> tc_order;               // tensor-core kernel instances, largest first
+  std::vector<int> tcb_order;              // N = 65 instances of the tensor-core border kernel
   int tc_smem = 0;
+  int tcb_smem = 0;
   int opt_pairs = 1;                       // LGB_OPT_TC_PAIRS
   int opt_waves = 1;                       // LGB_OPT_GEMM_WAVES
   int opt_stall = 0;                       // LGB_OPT_TEST_STALL
@@ -203,9 +207,9 @@ struct lgb_plan {
   void* blas_ws = nullptr;                 // cuBLAS workspace (graph capture allocates nothing)
   int smem_w = 0;
   int n_sm = 0;
-  cudaStream_t side[2] = {nullptr, nullptr};  // streams for kernels that run beside the first
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};  // streams for kernels that run beside the first
   cudaEvent_t ev_fork = nullptr;
-  cudaEvent_t ev_join[2] = {nullptr, nullptr};
+  cudaEvent_t ev_join[3] = {nullptr, nullptr, nullptr};
   std::vector<long long> off, doff, woff, soff;
   std::vector<unsigned char> place;
   long long tot_off = 0, tot_doff = 0, tot_woff = 0;
@@ -218,6 +222,7 @@ struct lgb_plan {
   int* d_order = nullptr;
   int* d_order_w = nullptr;
   int* d_tc_order = nullptr;
+  int* d_tcb_order = nullptr;
   int* d_queue = nullptr;
   long long* d_off = nullptr;
   long long* d_doff = nullptr;

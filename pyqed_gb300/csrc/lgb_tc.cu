@@ -942,7 +942,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
       case 16: tc_instance<BF16, 16, 1>(p, b, smem, sh, 0, phase, alive); break;
       case 32: tc_instance<BF16, 32, 1>(p, b, smem, sh, 0, phase, alive); break;
       case 48: tc_instance<BF16, 48, 1>(p, b, smem, sh, 0, phase, alive); break;
-      case kTcBorderNpad: tc_instance<BF16, 64, 1, true>(p, b, smem, sh, 0, phase, alive); break;
       default: tc_instance<BF16, 64, 1>(p, b, smem, sh, 0, phase, alive); break;
     }
   }
@@ -984,6 +983,35 @@ __global__ void __launch_bounds__(kThreads, 1) tc_rk4_kernel(CtaParams p, const 
   if (tid < 32) tmem_dealloc(sh.tmem_base, kTmemCols);
 }
 
+// N = 65 instances (64 x 64 block + SIMT border): one CTA each, a kernel of
+// their own so that the border's register pressure stays out of the
+// persistent kernel.  Launched ahead of it; the persistent CTAs take the
+// remaining SMs from the work queue.
+template <bool BF16>
+__global__ void __launch_bounds__(kThreads, 1) tc_border_kernel(CtaParams p, const int* order) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ TcShared sh;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&sh.mbar[0], 1);
+    mbar_init(&sh.mbar[1], 1);
+    mbar_fence_init();
+  }
+  if (tid < 32) {
+    tmem_alloc(&sh.tmem_base, kTmemCols);
+    tmem_relinquish();
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  uint32_t phase = 0;
+  bool alive = true;
+  tc_instance<BF16, 64, 1, true>(p, order[blockIdx.x], smem, sh, 0, phase, alive);
+  fence_before_sync();
+  __syncthreads();
+  if (tid < 32) tmem_dealloc(sh.tmem_base, kTmemCols);
+}
+
 }  // namespace
 
 int tc_max_dim() { return 64; }
@@ -1002,6 +1030,22 @@ int tc_smem_bytes(int precision, int npad) {
                                 (int)sizeof(TcBorder));
     default: return std::max(dual, bf16 ? (int)Geo<true, 64>::BYTES : (int)Geo<false, 64>::BYTES);
   }
+}
+
+cudaError_t launch_tc_border(const CtaParams& p, int precision, const int* order, int n_items,
+                             cudaStream_t stream) {
+  if (n_items <= 0) return cudaSuccess;
+  cudaError_t e;
+  if (precision == LGB_PREC_BF16X3) {
+    e = cudaFuncSetAttribute(tc_border_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem_bytes);
+    if (e != cudaSuccess) return e;
+    tc_border_kernel<true><<<n_items, kThreads, p.smem_bytes, stream>>>(p, order);
+  } else {
+    e = cudaFuncSetAttribute(tc_border_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem_bytes);
+    if (e != cudaSuccess) return e;
+    tc_border_kernel<false><<<n_items, kThreads, p.smem_bytes, stream>>>(p, order);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_tc_rk4(const CtaParams& p, int precision, const int* order, int n_items,
