@@ -525,6 +525,29 @@ def measure_heom(args, dev, n_inst=4096, n=8, nado=8, nt=1000, dt=0.01):
         out[key] = dict(seconds=best, instance_steps_per_s=n_inst * nt / best,
                         tflops=fl * n_inst * nt / best / 1e12, layout=plan.layout())
         plan.close()
+    # the reference's spin-boson setting as a parameter sweep: 65536 two-level
+    # systems (16 per warp), 10 levels, FP32, diagonal sz
+    nsb, sb_levels = 65536, 10
+    sb = W.heom_spin_boson()
+    rng = np.random.default_rng(17)
+    sbath = [bath_run(T, cu, lam) for T, cu, lam in zip(rng.uniform(0.5, 2.0, nsb), rng.uniform(0.2, 1.0, nsb),
+                                                        rng.uniform(0.01, 0.2, nsb))]
+    plan = _Plan([2] * nsb, nt, dt, sb_levels, 1, "fp32", C.HEOM_DIAG_SZ, dev)
+    plan.set(t(np.tile(sb["H"].ravel(), nsb)), t(np.tile(sb["sz"].ravel(), nsb)),
+             t(np.array([[g, d.real, d.imag] for g, d in sbath]).ravel()), t(np.tile(sb["sz"].T.ravel(), nsb)))
+    r0s = t(np.tile(sb["rho0"].ravel(), nsb))
+    res = plan.propagate(r0s)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    plan.propagate(r0s, out=res)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    plan.check_errors()
+    out["spinboson"] = dict(n_inst=nsb, N=2, nado=sb_levels, nt=nt, seconds=sec,
+                            instance_steps_per_s=nsb * nt / sec, layout=plan.layout())
+    plan.close()
     if not args.no_cpu:
         from oracle import heom_oracle as HO
         sample, steps = 16, 100
@@ -539,6 +562,14 @@ def measure_heom(args, dev, n_inst=4096, n=8, nado=8, nt=1000, dt=0.01):
             cpu_t += time.perf_counter() - t1
         out["cpu_baseline"] = dict(instance_steps_per_s=sample * steps / cpu_t, kind="port",
                                    sample="%d chains x %d sweeps, numpy complex128" % (sample, steps))
+        ado = np.zeros((sb_levels, 2, 2), complex)
+        ado[0] = sb["rho0"]
+        t1 = time.perf_counter()
+        for _ in range(200):
+            HO.sweep(ado, sb["H"], sb["sz"], sbath[0][0], sbath[0][1], dt)
+            np.trace(sb["sz"] @ ado[0])
+        out["spinboson"]["cpu_baseline"] = dict(instance_steps_per_s=200 / (time.perf_counter() - t1), kind="port",
+                                                sample="1 system x 200 sweeps, numpy complex128")
     out["note"] = ("one thread group per system (a warp: one thread per column and row pair), -iH, sz and "
                    "the %d levels in shared memory, one group barrier per level; flops per instance-step = "
                    "%d with the diagonal sz, %d with a dense sz (commutator products, 8 flops per complex "

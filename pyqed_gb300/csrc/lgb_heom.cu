@@ -225,10 +225,18 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
   __shared__ double red[2][kHWarps][kHMaxEops][2];
   const int G = p.G;
   const int g = threadIdx.x / G, gt = threadIdx.x - g * G;
-  const int b = blockIdx.x * p.gpc + g;
-  if (b >= p.n_inst) return;  // no CTA-wide barrier below: each group syncs on its own id
+  const int b_slot = blockIdx.x * p.gpc + g;
+  // G < 32: several systems share a warp (G a power of two) and sync with it
+  const bool sub = G < 32;
+  if (!sub && b_slot >= p.n_inst) return;  // no CTA-wide barrier below: each group syncs on its own
+  // a sub-warp group past the end of the batch repeats the last system with
+  // every global write off, so that all lanes keep taking part in the warp syncs
+  const bool active = b_slot < p.n_inst;
+  const int b = active ? b_slot : p.n_inst - 1;
   const int bid = 1 + g;
-  const bool wg = G == 32;  // a one-warp group syncs with warp primitives
+  const bool wg = G <= 32;  // a group within one warp syncs with warp primitives
+  const unsigned gmask = sub ? (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1))) : 0xffffffffu;
+  const int red0 = (G < 32 ? G : 32) >> 1;  // first offset of the in-group shuffle trees
   // NC > 0: every system has dimension NC (compile-time loops and strides)
   const int N = NC > 0 ? NC : p.dims[b], M = N * N, L = p.nado, NS = NC > 0 ? NC * NC : p.NS;
   const int h = (N + 1) >> 1, tasks = N * h;
@@ -254,7 +262,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
     }
   if constexpr (KAHAN)
     for (int i = gt; i < M; i += G) cmp[i] = mk<T2>(0.0, 0.0);
-  if (gt == 0) p.err[b] = 0;
+  if (gt == 0 && active) p.err[b] = 0;
   auto gsync = [&]() {
     if (wg) __syncwarp();
     else hbar(bid, G);
@@ -262,7 +270,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
   auto gsync_or = [&](bool pred) -> bool {
     if (wg) {
       __syncwarp();  // orders the level's shared-memory writes for the other lanes
-      return __any_sync(0xffffffffu, pred) != 0;
+      return __any_sync(gmask, pred) != 0;
     }
     return hbar_or(bid, G, pred);
   };
@@ -280,9 +288,9 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
     if constexpr (KAHAN) {
       if (wg && p.obs_out != nullptr) {
         __syncwarp();
-        for (int e = 0; e < E; ++e) {
+        for (int e = 0; e < E && active; ++e) {
           double2* row = p.obs_out + ((long long)b * E + e) * p.nt;
-          for (int st = lane; st < nsteps; st += 32) {
+          for (int st = gt; st < nsteps; st += G) {
             const float4 v = *reinterpret_cast<const float4*>(row + st);
             row[st] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
           }
@@ -386,6 +394,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
+              if (o > red0) continue;  // shuffles stay inside the group
               float s, er;
               two_sum(hx, __shfl_xor_sync(0xffffffffu, hx, o), s, er);
               lx += __shfl_xor_sync(0xffffffffu, lx, o) + er;
@@ -397,7 +406,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
             if (wg) {
               // staged as (hi, lo, hi, lo) in the 16-byte output slot and
               // widened to FP64 by whole warps after the run (flush_obs)
-              if (lane == 0 && p.obs_out != nullptr)
+              if (gt == 0 && active && p.obs_out != nullptr)
                 *reinterpret_cast<float4*>(p.obs_out + ((long long)b * E + e) * p.nt + step) =
                     make_float4(hx, lx, hyv, ly);
               continue;
@@ -421,17 +430,17 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
+              if (o > red0) continue;
               sx += __shfl_xor_sync(0xffffffffu, sx, o);
               sy += __shfl_xor_sync(0xffffffffu, sy, o);
             }
           }
-          if (lane == 0) {
-            if (wg) {
-              if (p.obs_out != nullptr) p.obs_out[((long long)b * E + e) * p.nt + step] = make_double2(sx, sy);
-            } else {
-              red[step & 1][warp][e][0] = sx;
-              red[step & 1][warp][e][1] = sy;
-            }
+          if (wg) {
+            if (gt == 0 && active && p.obs_out != nullptr)
+              p.obs_out[((long long)b * E + e) * p.nt + step] = make_double2(sx, sy);
+          } else if (lane == 0) {
+            red[step & 1][warp][e][0] = sx;
+            red[step & 1][warp][e][1] = sy;
           }
         }
         const bool bad = gsync_or(!fin);
@@ -444,9 +453,12 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
           p.obs_out[((long long)b * E + gt) * p.nt + step] = make_double2(sx, sy);
         }
         if (bad) {
-          if (gt == 0) p.err[b] = 4;  // LGB_ERR_NONFINITE
-          flush_obs(step + 1);
-          return;
+          if (gt == 0 && active) p.err[b] = 4;  // LGB_ERR_NONFINITE
+          if (!sub) {
+            flush_obs(step + 1);
+            return;
+          }
+          // a sub-warp group runs on with its warp; the error flag stands
         }
       } else {
         gsync();
@@ -460,6 +472,7 @@ __global__ void __launch_bounds__(kHThreads, sizeof(T) == 4 ? (DIAG ? 4 : 3) : 2
   }
   flush_obs(p.nt);
   // outputs: level n sits in slot (n - nt) mod L
+  if (!active) return;
   for (int l = 0; l < L; ++l) {
     const T2* X = lev + (size_t)ring(l - kk, L) * NS;
     for (int i = gt; i < M; i += G) {
@@ -588,7 +601,8 @@ int lgb_heom_create(lgb_heom_t* plan, const lgb_heom_problem_t* prob, const int3
   pl->NS = nmax * nmax;
   const bool uniform = std::all_of(pl->dims.begin(), pl->dims.end(), [&](int d) { return d == nmax; });
   if (uniform && (nmax == 2 || nmax == 4 || nmax == 8 || nmax == 16)) pl->nconst = nmax;
-  // one thread per (column, row pair) task
+  // one thread per (column, row pair) task; a batch of one small dimension
+  // (at most 16 tasks) packs 32 / G systems into each warp
   const int tasks = nmax * ((nmax + 1) / 2);
   pl->G = std::min(lgb::kHThreads, std::max(32, (tasks + 31) / 32 * 32));
   size_t per = heom_group_bytes(pl->NS, pr.nado, pr.precision, true);
@@ -597,6 +611,18 @@ int lgb_heom_create(lgb_heom_t* plan, const lgb_heom_problem_t* prob, const int3
     per = heom_group_bytes(pl->NS, pr.nado, pr.precision, false);
   }
   pl->gpc = std::max(1, std::min<int>(lgb::kHThreads / pl->G, (int)(lgb::kHSmemBudget / per)));
+  if (uniform && tasks <= 16 && pl->on_chip) {
+    int g = 1;
+    while (g < tasks) g <<= 1;
+    const int per_warp = 32 / g;
+    int gpc = std::min<int>(lgb::kHThreads / g, (int)(lgb::kHSmemBudget / per)) / per_warp * per_warp;
+    // no more whole warps than the batch fills
+    gpc = std::min(gpc, (pr.n_inst + per_warp - 1) / per_warp * per_warp);
+    if (gpc >= per_warp) {
+      pl->G = g;
+      pl->gpc = gpc;
+    }
+  }
   pl->smem = per * pl->gpc;
   bool ok = heom_upload(&pl->d_dims, pl->dims) && heom_upload(&pl->d_voff, pl->voff) &&
             cudaMalloc(&pl->d_bath, 3 * sizeof(double) * pr.n_inst) == cudaSuccess &&

@@ -147,8 +147,8 @@ def test_heom_layout_groups():
     H, sz, rho0, e_ops, bath = _ragged_batch(3, [4] * 20, 5)
     res = heom_batch(H, sz, rho0, e_ops, nado=5, dt=0.01, nt=3, bath=bath, precision="fp32")
     lay = res["layout"]
-    # N = 4: 8 (column, row pair) tasks, one warp per system
-    assert lay["on_chip"] and lay["threads_per_system"] == 32 and lay["systems_per_cta"] == 8
+    # N = 4: 8 (column, row pair) tasks, four systems per warp (20 systems: 5 warps' worth)
+    assert lay["on_chip"] and lay["threads_per_system"] == 8 and lay["systems_per_cta"] == 20
     H, sz, rho0, e_ops, bath = _ragged_batch(3, [16, 3], 5)
     lay = heom_batch(H, sz, rho0, e_ops, nado=5, dt=0.01, nt=3, bath=bath, precision="fp32")["layout"]
     assert lay["threads_per_system"] == 128 and lay["systems_per_cta"] == 2
@@ -201,3 +201,38 @@ def test_heom_compiled_dimensions_vs_oracle(N, sz_kind):
     for b in range(11):
         assert np.abs(res["observables"][b] - obs[b]).max() < TOL["fp32"]
         assert np.abs(res["ado"][b] - ados[b]).max() < TOL["fp32"]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("N,threads", [(1, 1), (2, 2), (3, 8), (5, 16)])
+def test_heom_small_systems_share_a_warp(prec, N, threads):
+    """Batches of one small dimension pack 32 / G systems into each warp; 37
+    systems leave idle groups in the last warp (they repeat the last system
+    with their writes off)."""
+    H, sz, rho0, e_ops, bath = _ragged_batch(50 + N, [N] * 37, 6)
+    dt, nt = 0.01, 150
+    res = heom_batch(H, sz, rho0, e_ops, nado=6, dt=dt, nt=nt, bath=bath, precision=prec, return_ado=True)
+    assert res["layout"]["threads_per_system"] == threads
+    obs, ados = _oracle_batch(H, sz, rho0, e_ops, bath, 6, dt, nt)
+    for b in range(37):
+        assert np.abs(res["observables"][b] - obs[b]).max() < TOL[prec], b
+        assert np.abs(res["ado"][b] - ados[b]).max() < TOL[prec], b
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_heom_small_systems_nonfinite_does_not_touch_warp_mates(prec):
+    H, sz, rho0, e_ops, bath = _ragged_batch(60, [2] * 20, 4)
+    rho0[5] = rho0[5].copy()
+    rho0[5][1, 1] = np.inf
+    plans = []
+    res = heom_batch(H, sz, rho0, e_ops, nado=4, dt=0.01, nt=30, bath=bath, precision=prec, _plan_out=plans)
+    flags = plans[0]
+    with pytest.raises(C.LindbladError) as ei:
+        flags.check_errors()
+    assert ei.value.status == C.LGB_ERR_NONFINITE and "system 5" in str(ei.value)
+    flags.close()
+    keep = [b for b in range(20) if b != 5]
+    obs, _ = _oracle_batch([H[b] for b in keep], [sz[b] for b in keep], [rho0[b] for b in keep],
+                           [e_ops[b] for b in keep], [bath[b] for b in keep], 4, 0.01, 30)
+    for k, b in enumerate(keep):
+        assert np.abs(res["observables"][b] - obs[k]).max() < TOL[prec], b
