@@ -466,8 +466,9 @@ def measure_redfield(args, dev, n_inst=2048, n=8, nt=1000, dt=0.1):
             cpu_t += time.perf_counter() - t1
         out["cpu_baseline"] = dict(instance_steps_per_s=sample * steps / cpu_t, kind="port",
                                    sample="%d chains x %d RK4 steps, numpy complex128" % (sample, steps))
-    out["note"] = ("one CTA per system, generator (64 x 64, FP32 32 KB / FP64 64 KB) in shared "
-                   "memory, warp-per-row GEMV per stage; flops = 32 N^4 per instance-step")
+    out["note"] = ("one CTA per system; FP32 (N^2 <= 64): the 64 x 64 generator in registers, four "
+                   "threads per row; FP64: the generator (64 KB) in shared memory, warp-per-row GEMV "
+                   "per stage; flops = 32 N^4 per instance-step")
     return out
 
 

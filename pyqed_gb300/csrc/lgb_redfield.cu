@@ -216,6 +216,162 @@ __global__ void __launch_bounds__(kRThreads) redfield_rk4_kernel(RedfieldParams 
 
 constexpr size_t kRSmemBudget = 200 * 1024;
 
+// FP32 systems with N^2 <= 64 (N <= 8): the generator lives in registers, four
+// threads per row of R, sixteen complex entries each; a stage is the partial
+// dot products of the four threads (the stage input broadcast from shared
+// memory), a two-step shuffle sum, and the RK4 combination by the row's
+// first thread, which keeps the row's state in registers.  One barrier per
+// stage (the stage input is double-buffered); a row's four threads take the
+// interleaved columns q, q + 4, .. so that their stage-input loads hit four
+// banks.  The same arithmetic as redfield_rk4_kernel<float>; observables are
+// reduced in FP32 with error-free TwoSum trees, staged as (hi, lo) pairs in
+// the output slots and widened to FP64 after the run.
+constexpr int kRRegM = 64;
+constexpr int kRRegCols = kRRegM / 4;
+
+__device__ __forceinline__ void rf_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__global__ void __launch_bounds__(kRThreads, 4) redfield_rk4_reg_kernel(RedfieldParams p) {
+  __shared__ float2 xs[2][kRRegM];
+  __shared__ float2 ots[kRMaxEops][kRRegM];
+  __shared__ float red[kRWarps][kRMaxEops][4];
+  const int b = blockIdx.x;
+  const int N = p.dims[b];
+  const int M = N * N;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int r = tid >> 2, q = tid & 3;
+  const int cpt = (M + 3) >> 2;  // columns per thread: q, q + 4, q + 8, ..
+  const bool owner = q == 0 && r < M;
+  const float2* Rg = reinterpret_cast<const float2*>(p.R) + p.roff[b];
+  float2 Rr[kRRegCols];
+#pragma unroll
+  for (int k = 0; k < kRRegCols; ++k) {
+    const int c = q + 4 * k;  // interleaved: the four threads of a row read four banks
+    Rr[k] = (r < M && k < cpt && c < M) ? Rg[(long long)r * M + c] : make_float2(0.f, 0.f);
+  }
+  const int E = p.n_eops;
+  const double2* Ot = p.Ot + (long long)E * p.voff[b];
+  for (int i = tid; i < kRMaxEops * kRRegM; i += kRThreads) {
+    const int e = i / kRRegM, j = i - e * kRRegM;
+    const double2 o = (e < E && j < M) ? Ot[(long long)e * M + j] : make_double2(0.0, 0.0);
+    ots[e][j] = make_float2((float)o.x, (float)o.y);
+  }
+  float2 y = make_float2(0.f, 0.f), acc = make_float2(0.f, 0.f);
+  if (owner) {
+    const double2 v = p.rho0[p.voff[b] + r];
+    y = make_float2((float)v.x, (float)v.y);
+  }
+  for (int i = tid; i < 2 * kRRegM; i += kRThreads) xs[i / kRRegM][i % kRRegM] = make_float2(0.f, 0.f);
+  __syncthreads();
+  if (owner) xs[0][r] = y;
+  if (tid == 0) p.err[b] = 0;
+  __syncthreads();
+  const float dt = (float)p.dt, hdt = (float)(0.5 * p.dt), sdt = (float)(p.dt / 6.0);
+  int cur = 0;
+  int nsteps = p.nt;  // steps whose observables were written
+  for (int step = 0; step < p.nt; ++step) {
+    for (int stage = 0; stage < 4; ++stage) {
+      float2 s = make_float2(0.f, 0.f);
+      const float2* x = xs[cur];
+#pragma unroll
+      for (int k = 0; k < kRRegCols; ++k)
+        if (k < cpt) cmac(s, Rr[k], x[q + 4 * k]);
+      s.x += __shfl_xor_sync(0xffffffffu, s.x, 1);
+      s.y += __shfl_xor_sync(0xffffffffu, s.y, 1);
+      s.x += __shfl_xor_sync(0xffffffffu, s.x, 2);
+      s.y += __shfl_xor_sync(0xffffffffu, s.y, 2);
+      if (owner) {
+        float2 xn;
+        if (stage == 0) {
+          acc = s;
+          xn = caxpy(y, hdt, s);
+        } else if (stage < 3) {
+          acc = caxpy(acc, 2.f, s);
+          xn = caxpy(y, stage == 2 ? dt : hdt, s);
+        } else {
+          float2 t = acc;
+          t.x += s.x;
+          t.y += s.y;
+          y = caxpy(y, sdt, t);
+          xn = y;
+        }
+        xs[cur ^ 1][r] = xn;
+      }
+      __syncthreads();
+      cur ^= 1;
+    }
+    // observables Tr[O rho] of rho(t_{step+1}) and its finiteness
+    const bool fin = !owner || (isfinite(y.x) && isfinite(y.y));
+#pragma unroll
+    for (int e = 0; e < kRMaxEops; ++e) {
+      if (e >= E) break;
+      float hx = 0.f, hy = 0.f, lx = 0.f, ly = 0.f;
+      if (owner) {
+        const float2 o = ots[e][r];
+        hx = fmaf(-o.y, y.y, o.x * y.x);
+        hy = fmaf(o.y, y.x, o.x * y.y);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        float sum, er;
+        rf_two_sum(hx, __shfl_xor_sync(0xffffffffu, hx, o), sum, er);
+        lx += __shfl_xor_sync(0xffffffffu, lx, o) + er;
+        hx = sum;
+        rf_two_sum(hy, __shfl_xor_sync(0xffffffffu, hy, o), sum, er);
+        ly += __shfl_xor_sync(0xffffffffu, ly, o) + er;
+        hy = sum;
+      }
+      if (lane == 0) {
+        red[warp][e][0] = hx;
+        red[warp][e][1] = lx;
+        red[warp][e][2] = hy;
+        red[warp][e][3] = ly;
+      }
+    }
+    if (p.store_every > 0 && p.states_out != nullptr && (step + 1) % p.store_every == 0 && owner) {
+      const long long ns = p.nt / p.store_every;
+      p.states_out[p.voff[b] * ns + (long long)((step + 1) / p.store_every - 1) * M + r] =
+          make_double2(y.x, y.y);
+    }
+    const bool bad = __syncthreads_or(!fin) != 0;
+    if (tid < E && p.obs_out != nullptr) {
+      // FP32 (hi, lo) sums across the warps, staged in the 16-byte output
+      // slot; widened to FP64 after the run (no FP64 arithmetic per step)
+      float hx = red[0][tid][0], lx = red[0][tid][1], hy = red[0][tid][2], ly = red[0][tid][3];
+      for (int w = 1; w < kRWarps; ++w) {
+        float sum, er;
+        rf_two_sum(hx, red[w][tid][0], sum, er);
+        lx += red[w][tid][1] + er;
+        hx = sum;
+        rf_two_sum(hy, red[w][tid][2], sum, er);
+        ly += red[w][tid][3] + er;
+        hy = sum;
+      }
+      *reinterpret_cast<float4*>(p.obs_out + ((long long)b * p.nt + step) * E + tid) = make_float4(hx, lx, hy, ly);
+    }
+    if (bad) {
+      if (tid == 0) p.err[b] = 4;  // LGB_ERR_NONFINITE
+      nsteps = step + 1;
+      break;
+    }
+    __syncthreads();
+  }
+  if (p.obs_out != nullptr) {
+    __syncthreads();
+    double2* o = p.obs_out + (long long)b * p.nt * E;
+    for (long long i = tid; i < (long long)nsteps * E; i += kRThreads) {
+      const float4 v = *reinterpret_cast<const float4*>(o + i);
+      o[i] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+    }
+  }
+  if (nsteps < p.nt) return;
+  if (p.rho_out != nullptr && owner) p.rho_out[p.voff[b] + r] = make_double2(y.x, y.y);
+}
+
 }  // namespace
 }  // namespace lgb
 
@@ -227,6 +383,7 @@ struct lgb_redfield_plan {
   std::vector<unsigned char> rsm;
   long long tot_r = 0, tot_v = 0;
   size_t smem = 0;
+  bool reg = false;  // FP32 and every N^2 <= 64: the register-resident kernel
   int* d_dims = nullptr;
   long long* d_roff = nullptr;
   long long* d_voff = nullptr;
@@ -301,6 +458,8 @@ int lgb_redfield_create(lgb_redfield_t* plan, const lgb_redfield_problem_t* prob
     pl->rsm.push_back(in_smem ? 1 : 0);
     pl->smem = std::max(pl->smem, vec + (in_smem ? gen : 0));
   }
+  pl->reg = pr.precision == LGB_PREC_FP32 &&
+            std::all_of(pl->dims.begin(), pl->dims.end(), [](int d) { return d * d <= lgb::kRRegM; });
   bool ok = rf_upload(&pl->d_dims, pl->dims) && rf_upload(&pl->d_roff, pl->roff) &&
             rf_upload(&pl->d_voff, pl->voff) && rf_upload(&pl->d_rsm, pl->rsm) &&
             cudaMalloc(&pl->d_R, std::max<long long>(1, pl->tot_r) * esz) == cudaSuccess &&
@@ -376,6 +535,9 @@ int lgb_redfield_propagate(lgb_redfield_t plan, const double* rho0, double* obs_
                              (int)plan->smem);
     if (e == cudaSuccess)
       lgb::redfield_rk4_kernel<double><<<pr.n_inst, lgb::kRThreads, plan->smem, st>>>(p);
+  } else if (plan->reg) {
+    lgb::redfield_rk4_reg_kernel<<<pr.n_inst, lgb::kRThreads, 0, st>>>(p);
+    e = cudaSuccess;
   } else {
     e = cudaFuncSetAttribute(lgb::redfield_rk4_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)plan->smem);

@@ -46,10 +46,11 @@ def test_redfield_gue_golden(golden, prec, tol):
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 1e-5)])
-def test_redfield_batch_uneven_vs_oracle(prec, tol):
-    # N = 16 keeps the generator in L2 (streamed) in both precisions, N <= 6 in shared memory
-    rng = np.random.default_rng(4)
-    dims = [3, 6, 11, 16]
+@pytest.mark.parametrize("dims", [[3, 6, 11, 16], [1, 2, 5, 8, 7, 8]])
+def test_redfield_batch_uneven_vs_oracle(prec, tol, dims):
+    # N = 16 keeps the generator in L2 (streamed) in both precisions, N <= 6 in
+    # shared memory; a batch with every N <= 8 runs FP32 with R in registers
+    rng = np.random.default_rng(4 + len(dims))
     H, A, S, R0, E = [], [], [], [], []
     for N in dims:
         h = W.gue_matrix(rng, N) * 0.5
@@ -69,3 +70,22 @@ def test_redfield_batch_uneven_vs_oracle(prec, tol):
         assert np.abs(res["rho"][b] - rholist[-1]).max() < tol
         for k in range(3):
             assert np.abs(res["states"][b][k] - rholist[20 * k + 19]).max() < tol
+
+
+def test_redfield_fp32_register_kernel_nonfinite():
+    """A non-finite state stops its own system only (register-resident kernel)."""
+    rng = np.random.default_rng(9)
+    dims = [4, 8, 6]
+    H, A, S, R0, E = [], [], [], [], []
+    for N in dims:
+        h = W.gue_matrix(rng, N) * 0.5
+        H.append(h), A.append([np.diag(rng.uniform(-1, 1, N)).astype(complex)])
+        S.append([W.ohmic_spectrum(0.05, 0.8, 3.0)])
+        psi = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        R0.append(np.outer(psi, psi.conj()) / np.vdot(psi, psi).real), E.append([h])
+    R0[1] = R0[1].copy()
+    R0[1][0, 0] = np.nan
+    from pyqed_gb300 import _capi as C
+    with pytest.raises(C.LindbladError) as ei:
+        redfield_batch(H, A, S, R0, 0.05, 10, e_ops=E, precision="fp32")
+    assert ei.value.status == C.LGB_ERR_NONFINITE and "system 1" in str(ei.value)
