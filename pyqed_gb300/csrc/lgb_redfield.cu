@@ -235,16 +235,17 @@ __device__ __forceinline__ void rf_two_sum(float a, float b, float& s, float& e)
   e = (a - (s - bb)) + (b - bb);
 }
 
+template <int MC>  // MC > 0: every system has N^2 = MC (compile-time column loop)
 __global__ void __launch_bounds__(kRThreads, 4) redfield_rk4_reg_kernel(RedfieldParams p) {
   __shared__ float2 xs[2][kRRegM];
   __shared__ float2 ots[kRMaxEops][kRRegM];
   __shared__ float red[kRWarps][kRMaxEops][4];
   const int b = blockIdx.x;
   const int N = p.dims[b];
-  const int M = N * N;
+  const int M = MC > 0 ? MC : N * N;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r = tid >> 2, q = tid & 3;
-  const int cpt = (M + 3) >> 2;  // columns per thread: q, q + 4, q + 8, ..
+  const int cpt = MC > 0 ? (MC + 3) / 4 : (M + 3) >> 2;  // columns per thread: q, q + 4, q + 8, ..
   const bool owner = q == 0 && r < M;
   const float2* Rg = reinterpret_cast<const float2*>(p.R) + p.roff[b];
   float2 Rr[kRRegCols];
@@ -275,11 +276,13 @@ __global__ void __launch_bounds__(kRThreads, 4) redfield_rk4_reg_kernel(Redfield
   int nsteps = p.nt;  // steps whose observables were written
   for (int step = 0; step < p.nt; ++step) {
     for (int stage = 0; stage < 4; ++stage) {
-      float2 s = make_float2(0.f, 0.f);
       const float2* x = xs[cur];
+      // four independent accumulators (short dependency chains)
+      float2 s4[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
       for (int k = 0; k < kRRegCols; ++k)
-        if (k < cpt) cmac(s, Rr[k], x[q + 4 * k]);
+        if (k < cpt) cmac(s4[k & 3], Rr[k], x[q + 4 * k]);
+      float2 s = make_float2((s4[0].x + s4[1].x) + (s4[2].x + s4[3].x), (s4[0].y + s4[1].y) + (s4[2].y + s4[3].y));
       s.x += __shfl_xor_sync(0xffffffffu, s.x, 1);
       s.y += __shfl_xor_sync(0xffffffffu, s.y, 1);
       s.x += __shfl_xor_sync(0xffffffffu, s.x, 2);
@@ -536,7 +539,11 @@ int lgb_redfield_propagate(lgb_redfield_t plan, const double* rho0, double* obs_
     if (e == cudaSuccess)
       lgb::redfield_rk4_kernel<double><<<pr.n_inst, lgb::kRThreads, plan->smem, st>>>(p);
   } else if (plan->reg) {
-    lgb::redfield_rk4_reg_kernel<<<pr.n_inst, lgb::kRThreads, 0, st>>>(p);
+    const bool all8 = std::all_of(plan->dims.begin(), plan->dims.end(), [](int d) { return d == 8; });
+    if (all8)
+      lgb::redfield_rk4_reg_kernel<64><<<pr.n_inst, lgb::kRThreads, 0, st>>>(p);
+    else
+      lgb::redfield_rk4_reg_kernel<0><<<pr.n_inst, lgb::kRThreads, 0, st>>>(p);
     e = cudaSuccess;
   } else {
     e = cudaFuncSetAttribute(lgb::redfield_rk4_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
