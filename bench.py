@@ -422,12 +422,13 @@ def measure_redfield(args, dev, n_inst=2048, n=8, nt=1000, dt=0.1):
     oracle's numpy rate for the same algorithm on a sample."""
     import torch
     from pyqed_gb300 import workloads as W
-    from pyqed_gb300.redfield import _Plan, _eigen_parts, build_tensor
+    from pyqed_gb300.redfield import _Plan, _eigen_parts, build_tensors
     chains = [W.redfield_chain(n=n, seed=100 + b) for b in range(n_inst)]
     parts = [_eigen_parts(c["H"], c["a_ops"], c["spectra"]) for c in chains]
+    build_tensors(parts[:2], dev)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    R = torch.cat([build_tensor(p[0], p[2], p[3], dev) for p in parts])
+    R = build_tensors(parts, dev)
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
     Ot = np.concatenate([np.concatenate([(p[1].conj().T @ e @ p[1]).T.flatten() for e in c["e_ops"]])

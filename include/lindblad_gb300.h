@@ -211,6 +211,13 @@ int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value);
 int lgb_redfield_tensor(int32_t n, int32_t n_ops, const double* evals, const double* A,
                         const double* C, double* R_out, void* stream);
 
+/* The generators of n_sys systems in one launch: dims_host[n_sys] (host),
+ * evals packed (system b at sum_{c<b} N_c), A and C packed n_ops x N_b^2 at
+ * n_ops * sum_{c<b} N_c^2, R_out packed N_b^4 at sum_{c<b} N_c^4.  Device
+ * pointers for the data.  Synchronous: returns when the generators are built. */
+int lgb_redfield_tensor_batch(int32_t n_sys, const int32_t* dims_host, int32_t n_ops, const double* evals,
+                              const double* A, const double* C, double* R_out, void* stream);
+
 /* Largest supported dimension per precision (64 for FP32, 48 for FP64). */
 int lgb_redfield_max_dim(int32_t precision);
 

@@ -40,7 +40,7 @@ EXPORTS = [
     "lgb_get_version", "lgb_status_string", "lgb_plan_create", "lgb_plan_destroy",
     "lgb_plan_set_operators", "lgb_plan_propagate", "lgb_plan_errors", "lgb_plan_get_info",
     "lgb_propagate_noalloc", "lgb_plan_adjoint", "lgb_plan_set_option",
-    "lgb_redfield_tensor", "lgb_redfield_max_dim", "lgb_redfield_create", "lgb_redfield_destroy",
+    "lgb_redfield_tensor", "lgb_redfield_tensor_batch", "lgb_redfield_max_dim", "lgb_redfield_create", "lgb_redfield_destroy",
     "lgb_redfield_set", "lgb_redfield_propagate", "lgb_redfield_errors",
     "lgb_heom_max_dim", "lgb_heom_max_levels_on_chip", "lgb_heom_create", "lgb_heom_destroy",
     "lgb_heom_layout", "lgb_heom_set", "lgb_heom_propagate", "lgb_heom_errors",
@@ -136,6 +136,8 @@ def lib():
     L.lgb_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
     L.lgb_redfield_tensor.restype = ctypes.c_int
     L.lgb_redfield_tensor.argtypes = [i32, i32, dp, dp, dp, dp, vp]
+    L.lgb_redfield_tensor_batch.restype = ctypes.c_int
+    L.lgb_redfield_tensor_batch.argtypes = [i32, ctypes.POINTER(i32), i32, dp, dp, dp, dp, vp]
     L.lgb_redfield_max_dim.restype = ctypes.c_int
     L.lgb_redfield_max_dim.argtypes = [i32]
     L.lgb_redfield_create.restype = ctypes.c_int

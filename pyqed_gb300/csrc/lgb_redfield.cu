@@ -74,6 +74,55 @@ __global__ void redfield_tensor_kernel(int n, int K, const double* evals, const 
   }
 }
 
+// Generators of many systems in one launch: blockIdx.y is the system, whose
+// eigenvalues, operators, spectra and R start at the given offsets.
+__global__ void redfield_tensor_batch_kernel(int K, const int* dims, const long long* eoff, const long long* moff,
+                                             const long long* roff, const double* evals, const double2* A,
+                                             const double* C, double2* R) {
+  const int sys = blockIdx.y;
+  const int n = dims[sys];
+  const long long M = (long long)n * n, total = M * M, nn = M;
+  const double* ev = evals + eoff[sys];
+  const double2* As = A + (long long)K * moff[sys];
+  const double* Cs = C + (long long)K * moff[sys];
+  double2* Rs = R + roff[sys];
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(idx / M), q = (int)(idx % M);
+    const int a = r / n, b = r % n, x = q / n, y = q % n;
+    double vx = 0.0, vy = 0.0;
+    if (a == x && b == y) vy = -(ev[a] - ev[b]);
+    for (int k = 0; k < K; ++k) {
+      const double2* Ak = As + k * nn;
+      const double* Ck = Cs + k * nn;
+      const double2 Aax = Ak[a * n + x], Ayb = Ak[y * n + b];
+      const double cax = Ck[a * n + x], cby = Ck[b * n + y];
+      const double2 Lax = make_double2(cax * Aax.x, cax * Aax.y);
+      const double2 Aby = Ak[b * n + y];
+      const double2 Ldyb = make_double2(cby * Aby.x, -cby * Aby.y);
+      vx += Aax.x * Ldyb.x - Aax.y * Ldyb.y + Lax.x * Ayb.x - Lax.y * Ayb.y;
+      vy += Aax.x * Ldyb.y + Aax.y * Ldyb.x + Lax.x * Ayb.y + Lax.y * Ayb.x;
+      if (b == y) {
+        for (int c = 0; c < n; ++c) {
+          const double2 Aac = Ak[a * n + c], Acx = Ak[c * n + x];
+          const double ccx = Ck[c * n + x];
+          vx -= ccx * (Aac.x * Acx.x - Aac.y * Acx.y);
+          vy -= ccx * (Aac.x * Acx.y + Aac.y * Acx.x);
+        }
+      }
+      if (a == x) {
+        for (int c = 0; c < n; ++c) {
+          const double2 Acy = Ak[c * n + y], Acb = Ak[c * n + b];
+          const double ccy = Ck[c * n + y];
+          vx -= ccy * (Acy.x * Acb.x + Acy.y * Acb.y);
+          vy -= ccy * (Acy.x * Acb.y - Acy.y * Acb.x);
+        }
+      }
+    }
+    Rs[idx] = make_double2(vx, vy);
+  }
+}
+
 template <typename T>
 __global__ void redfield_convert_kernel(const double2* src, typename Cplx<T>::type* dst, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -429,6 +478,55 @@ int lgb_redfield_tensor(int32_t n, int32_t n_ops, const double* evals, const dou
   lgb::redfield_tensor_kernel<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
       n, n_ops, evals, reinterpret_cast<const double2*>(A), C, reinterpret_cast<double2*>(R_out));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
+int lgb_redfield_tensor_batch(int32_t n_sys, const int32_t* dims_host, int32_t n_ops, const double* evals,
+                              const double* A, const double* C, double* R_out, void* stream) {
+  if (n_sys < 1 || dims_host == nullptr || n_ops < 0 || evals == nullptr || R_out == nullptr ||
+      (n_ops > 0 && (A == nullptr || C == nullptr)))
+    return LGB_ERR_INVALID_ARG;
+  std::vector<int> dims(n_sys);
+  std::vector<long long> eoff(n_sys), moff(n_sys), roff(n_sys);
+  long long te = 0, tm = 0, tr = 0, maxr = 1;
+  for (int b = 0; b < n_sys; ++b) {
+    const int n = dims_host[b];
+    if (n < 1 || n > lgb_redfield_max_dim(LGB_PREC_FP32)) return LGB_ERR_INVALID_ARG;
+    dims[b] = n;
+    eoff[b] = te;
+    moff[b] = tm;
+    roff[b] = tr;
+    te += n;
+    tm += (long long)n * n;
+    tr += (long long)n * n * n * n;
+    maxr = std::max(maxr, (long long)n * n * n * n);
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int* d_dims = nullptr;
+  long long* d_off = nullptr;
+  if (cudaMallocAsync(&d_dims, n_sys * sizeof(int), st) != cudaSuccess) return LGB_ERR_CUDA;
+  if (cudaMallocAsync(&d_off, 3 * (size_t)n_sys * sizeof(long long), st) != cudaSuccess) {
+    cudaFreeAsync(d_dims, st);
+    return LGB_ERR_CUDA;
+  }
+  std::vector<long long> offs;
+  offs.insert(offs.end(), eoff.begin(), eoff.end());
+  offs.insert(offs.end(), moff.begin(), moff.end());
+  offs.insert(offs.end(), roff.begin(), roff.end());
+  bool ok = cudaMemcpyAsync(d_dims, dims.data(), n_sys * sizeof(int), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(d_off, offs.data(), offs.size() * sizeof(long long), cudaMemcpyHostToDevice, st) ==
+                cudaSuccess;
+  if (ok) {
+    const int gx = (int)std::min<long long>((maxr + 255) / 256, 64);
+    lgb::redfield_tensor_batch_kernel<<<dim3(gx, n_sys), 256, 0, st>>>(
+        n_ops, d_dims, d_off, d_off + n_sys, d_off + 2 * n_sys, evals, reinterpret_cast<const double2*>(A), C,
+        reinterpret_cast<double2*>(R_out));
+    ok = cudaGetLastError() == cudaSuccess;
+  }
+  // the host vectors must outlive the asynchronous copies
+  cudaStreamSynchronize(st);
+  cudaFreeAsync(d_dims, st);
+  cudaFreeAsync(d_off, st);
+  return ok ? LGB_OK : LGB_ERR_CUDA;
 }
 
 int lgb_redfield_max_dim(int32_t precision) { return precision == LGB_PREC_FP64 ? 48 : 64; }

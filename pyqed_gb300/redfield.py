@@ -23,7 +23,7 @@ from . import _capi as C
 from .engine import _device, to_dense
 from .mol import Result
 
-__all__ = ["RedfieldSolver", "redfield_batch", "build_tensor"]
+__all__ = ["RedfieldSolver", "redfield_batch", "build_tensor", "build_tensors"]
 
 _PREC = {"fp64": C.PREC["fp64"], "fp32": C.PREC["fp32"]}
 
@@ -67,6 +67,29 @@ def build_tensor(evals, A, Cs, device=None):
         C.check(L.lgb_redfield_tensor(N, len(A), _ptr(ev), _ptr(At), _ptr(Ct), _ptr(R),
                                       ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)),
                 "lgb_redfield_tensor")
+    return R
+
+
+def build_tensors(parts, device=None):
+    """Generators of many systems (``_eigen_parts`` results with the same
+    operator count) in one launch (``lgb_redfield_tensor_batch``): packed
+    complex128 on the device, system b at sum_{c<b} N_c^4."""
+    dev = _device(device)
+    dims = [len(p[0]) for p in parts]
+    K = parts[0][2].shape[0]
+    if any(p[2].shape[0] != K for p in parts):
+        return torch.cat([build_tensor(p[0], p[2], p[3], dev) for p in parts])
+    L = C.lib()
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)  # noqa: E731
+    ev = t(np.concatenate([p[0] for p in parts]), np.float64)
+    At = t(np.concatenate([p[2].ravel() for p in parts]) if K else np.zeros(0), np.complex128)
+    Ct = t(np.concatenate([p[3].ravel() for p in parts]) if K else np.zeros(0), np.float64)
+    R = torch.empty(int(sum(n ** 4 for n in dims)), dtype=torch.complex128, device=dev)
+    with torch.cuda.device(dev):
+        C.check(L.lgb_redfield_tensor_batch(len(dims), (ctypes.c_int32 * len(dims))(*dims), K, _ptr(ev), _ptr(At),
+                                            _ptr(Ct), _ptr(R),
+                                            ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)),
+                "lgb_redfield_tensor_batch")
     return R
 
 
@@ -206,7 +229,7 @@ def redfield_batch(H, a_ops, spectra, rho0, dt, Nt, e_ops=None, *, precision="fp
     dims = [len(p[0]) for p in parts]
     plan = _Plan(dims, Nt, dt, E, precision, store_every, device)
     try:
-        R = torch.cat([build_tensor(p[0], p[2], p[3], plan.dev) for p in parts])
+        R = build_tensors(parts, plan.dev)
         Ot = np.concatenate([np.concatenate([(p[1].conj().T @ to_dense(e) @ p[1]).T.flatten()
                                              for e in e_ops[b]]) if E else np.zeros(0, complex)
                              for b, p in enumerate(parts)])

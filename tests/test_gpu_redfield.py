@@ -89,3 +89,16 @@ def test_redfield_fp32_register_kernel_nonfinite():
     with pytest.raises(C.LindbladError) as ei:
         redfield_batch(H, A, S, R0, 0.05, 10, e_ops=E, precision="fp32")
     assert ei.value.status == C.LGB_ERR_NONFINITE and "system 1" in str(ei.value)
+
+
+def test_redfield_batched_tensor_build_matches_single():
+    from pyqed_gb300.redfield import _eigen_parts, build_tensor, build_tensors
+    parts = [_eigen_parts(c["H"], c["a_ops"], c["spectra"])
+             for c in (W.redfield_chain(n=n, seed=s) for n, s in ((3, 1), (6, 2), (8, 3), (5, 4)))]
+    Rb = build_tensors(parts).cpu().numpy()
+    off = 0
+    for p in parts:
+        n = len(p[0])
+        R1 = build_tensor(p[0], p[2], p[3]).cpu().numpy()
+        assert np.array_equal(Rb[off:off + n ** 4], R1)
+        off += n ** 4
