@@ -578,10 +578,14 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         const int row = d & (kG - 1);
         const bool t4 = d >= kG;
         float sx = 0.f, sy = 0.f;
-#pragma unroll 4
+        // all sixteen loads of A (L2-resident) in flight at once
+        float2 av[16];
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) av[kk] = __ldg(At0 + (q * 16 + kk) * NPS + row);  // A[row][k]
+#pragma unroll
         for (int kk = 0; kk < 16; ++kk) {
           const int k = q * 16 + kk;
-          const float2 a = At0[k * NPS + row];  // A[row][k]
+          const float2 a = av[kk];
           const float2 v = t4 ? br[k] : bc[k];
           const float ay = t4 ? -a.y : a.y;
           sx = fmaf(a.x, v.x, fmaf(-ay, v.y, sx));
