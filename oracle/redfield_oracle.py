@@ -8,6 +8,9 @@ Follows binggu56/pyqed 0.1.3:
   * ``_redfield``         ``pyqed/oqs.py:364-459`` (the ``return_result`` branch)
   * ``rk4``               ``pyqed/phys.py:1051-1064``; ``transform`` ``:1121-1140``;
     ``obs_dm`` ``:1257-1264``
+  * ``RedfieldSolver.propagator`` / ``expect`` / ``correlation_4op_3t``
+                          ``pyqed/oqs.py:161-330`` (with ``expm``
+    ``pyqed/phys.py:2049-2097`` for the 'EOM' propagator)
 Pinned by ``tests/golden/redfield*.npz`` (outputs of the reference itself).
 """
 import numpy as np
@@ -39,7 +42,8 @@ def redfield_tensor(H, a_ops, spectra):
     for a in a_ops:
         if not np.allclose(a, _dag(a)):
             raise TypeError("Operators in a_ops must be Hermitian.")
-    evals, evecs = np.linalg.eigh(H)
+    import scipy.linalg
+    evals, evecs = scipy.linalg.eigh(H)  # the reference's eigensolver: eigenbasis quantities depend on its signs
     W = np.real(evals[:, None] - evals[None, :])
     N = len(evals)
     R = -1j * _op2sop(np.diag(evals))
@@ -93,3 +97,54 @@ def redfield_propagate(R, rho0, evecs, Nt, dt, e_ops=()):
         rholist.append(evecs @ tmp @ _dag(evecs))
         obs[k, :] = [np.trace(e @ tmp) for e in es]
     return obs, rholist, r0
+
+
+def propagator_sos(R, t):
+    """U(t_k) = U1 exp(lambda t_k) U1^-1, (M, M, len(t)) (``propagator`` 'SOS')."""
+    import scipy.linalg
+    evals, U1 = scipy.linalg.eig(R)
+    U2 = scipy.linalg.inv(U1)
+    E = np.exp(evals[:, None] * np.asarray(t)[None, :])
+    return np.einsum('aj,jk,jb->abk', U1, E, U2)
+
+
+def propagator_eom(R, t):
+    """RK4 steps of dU/dt = R U from the identity with dt = t[1] - t[0]
+    (``expm`` 'EOM', ``pyqed/phys.py:2081-2097``)."""
+    M = R.shape[0]
+    U = np.eye(M, dtype=complex)
+    out = []
+    dt = t[1] - t[0] if len(t) > 1 else 0.0
+    for _ in range(len(t)):
+        out.append(U.copy())
+        U = rk4_vec(U, R, dt)
+    return np.dstack(out)
+
+
+def expect(U, rho0, evecs, e_ops):
+    """``RedfieldSolver.expect`` with an ndarray propagator: sum_ab e_ab rho_ab(t)
+    in the eigenbasis (``pyqed/oqs.py:319-344``)."""
+    r0 = (_dag(evecs) @ rho0 @ evecs).flatten()
+    rho = np.tensordot(U, r0, axes=([1], [0]))
+    return np.stack([(_dag(evecs) @ e @ evecs).flatten() @ rho for e in e_ops], axis=1)
+
+
+def superop(a, kind):
+    n = a.shape[-1]
+    i = np.eye(n)
+    return {"l": np.kron(a, i), "r": np.kron(i, a.T), "c": np.kron(a, i) - np.kron(i, a.T),
+            "a": np.kron(a, i) + np.kron(i, a.T)}[kind]
+
+
+def correlation_4op_3t(G, rho0, oplist, signature):
+    """``RedfieldSolver.correlation_4op_3t`` (``pyqed/oqs.py:239-330``) with the
+    Green's function G (M, M, T): (tau3, tau2, tau1)."""
+    a, b, c, d = (superop(o, s) for o, s in zip(oplist, signature))
+    n = rho0.shape[0]
+    rho = d @ rho0.flatten()
+    tmp = np.tensordot(G, rho, axes=(1, 0))
+    tmp = c @ tmp
+    tmp = np.tensordot(G, tmp, axes=([1], [0]))
+    tmp = np.tensordot(b, tmp, axes=([1], [0]))
+    tmp = np.tensordot(G, tmp, axes=([1], [0]))
+    return np.einsum('a,ab,bijk->ijk', np.eye(n).flatten(), a, tmp)

@@ -17,6 +17,7 @@ from __future__ import annotations
 import ctypes
 
 import numpy as np
+import scipy.linalg
 import torch
 
 from . import _capi as C
@@ -44,7 +45,9 @@ def _eigen_parts(H, a_ops, spectra):
     H = to_dense(H)
     a_ops = [to_dense(a) for a in a_ops]
     _herm_check(a_ops)
-    evals, evecs = np.linalg.eigh(H)
+    # the reference's eigensolver (scipy.linalg.eigh): R, the propagator and
+    # every other eigenbasis quantity depend on the signs it picks
+    evals, evecs = scipy.linalg.eigh(H)
     W = np.real(evals[:, None] - evals[None, :])
     N = len(evals)
     A = np.stack([evecs.conj().T @ a @ evecs for a in a_ops]) if a_ops else np.zeros((0, N, N), complex)
@@ -145,7 +148,18 @@ class _Plan:
 
 
 class RedfieldSolver:
-    """``pyqed.oqs.RedfieldSolver`` on the GPU (``pyqed/oqs.py:30-100``)."""
+    """``pyqed.oqs.RedfieldSolver`` on the GPU (``pyqed/oqs.py:30-360``).
+
+    Beside ``evolve``: ``propagator`` (the Liouville-space propagator U(t) in
+    the eigenbasis; 'SOS' by the eigendecomposition of R, 'EOM' by RK4 with
+    dt = t[1] - t[0] on the batched RK4 kernel, one system per basis vector),
+    ``gf`` (G(t) = -i U(t)), ``expect``, ``correlation_2op_1t`` and
+    ``correlation_4op_3t`` (``pyqed/oqs.py:136-330``).  Deviations, where the
+    reference's method cannot run: ``gf(method='EOM')`` returns -i U(t) (the
+    reference multiplies a list by -1j), ``correlation_2op_1t`` returns
+    <<1| a G(tau) b |rho0>> (the reference's vector shapes do not match),
+    ``steady_state`` returns the normalised null vector of R in the original
+    basis (the reference's takes no ``self``)."""
 
     def __init__(self, H, c_ops=None, spectra=None, e_ops=None):
         self.H = H
@@ -158,6 +172,8 @@ class RedfieldSolver:
         self.G = None
         self.e_ops = e_ops
         self._Rdev = None
+        self.U = None
+        self.G = None
 
     def idm(self, sp=True):
         """vec of the identity in Liouville space (row-major)."""
@@ -183,6 +199,118 @@ class RedfieldSolver:
         self.R = csr_matrix(self._Rdev.cpu().numpy().reshape(N * N, N * N))
         self.evecs = evecs
         return self.R, evecs
+
+    # ---- Liouville-space propagator and correlations (pyqed/oqs.py:133-330) -------
+    def _dense_R(self):
+        return self._Rdev.reshape(self.dim ** 2, self.dim ** 2)
+
+    def propagator(self, t, method='SOS'):
+        """U(t_k) (M x M x len(t), eigenbasis, M = N^2); also sets ``U`` and
+        ``G = -1j U``."""
+        if self.R is None:
+            raise TypeError('Redfield tensor is not computed. Please call redfield_tensor()')
+        t = np.asarray(t, dtype=float)
+        M = self.dim ** 2
+        dev = self._Rdev.device
+        if method == 'EOM':
+            # RK4 with dt = t[1] - t[0] from the identity: the M basis vectors
+            # as a batch of systems sharing R, every state kept
+            nt = len(t) - 1
+            U = np.zeros((M, M, len(t)), dtype=complex)
+            U[:, :, 0] = np.eye(M)
+            if nt > 0:
+                plan = _Plan([self.dim] * M, nt, float(t[1] - t[0]), 0, "fp64", 1, dev)
+                try:
+                    plan.set(self._Rdev.repeat(M), torch.zeros(0, dtype=torch.complex128, device=dev))
+                    r0 = torch.eye(M, dtype=torch.complex128, device=dev).reshape(-1)
+                    _, _, st = plan.propagate(r0, want_states=True)
+                finally:
+                    plan.close()
+                # system c holds nt consecutive states: U[:, c, k + 1]
+                U[:, :, 1:] = st.reshape(M, nt, M).permute(2, 0, 1).cpu().numpy()
+        elif method in ['eseries', 'SOS']:
+            evals, U1 = scipy.linalg.eig(self.R.toarray())
+            U2 = scipy.linalg.inv(U1)
+            td = torch.from_numpy(t).to(dev)
+            lam = torch.from_numpy(evals).to(dev)
+            A = torch.from_numpy(U1).to(dev)
+            B = torch.from_numpy(U2).to(dev)
+            E = torch.exp(lam[None, :] * td[:, None])              # (T, M)
+            U = ((A[None, :, :] * E[:, None, :]) @ B[None]).permute(1, 2, 0).cpu().numpy()
+        else:
+            raise ValueError('method must be EOM, SOS or eseries')
+        self.U = U
+        self.G = -1j * self.U
+        return self.U
+
+    def gf(self, t, w=None, secular=False, k=1, domain='time', method='EOM'):
+        """Liouville-space Green's function G(t) = -i U(t), M x M x len(t)."""
+        if self.R is None:
+            self.redfield_tensor(secular=secular)
+        if method == 'EOM':
+            return -1j * self.propagator(t, method='EOM')
+        if method in ['eseries', 'diag', 'diagonalization']:
+            return -1j * self.propagator(np.asarray(t, dtype=float), method='SOS')
+        raise ValueError('method must be EOM, eseries, diag or diagonalization')
+
+    def expect(self, rho0, e_ops):
+        """sum_ab e_ab rho_ab(t) in the eigenbasis for every t of the last
+        ``propagator`` (the reference's contraction, ``pyqed/oqs.py:319-344``)."""
+        V = self.evecs
+        r0 = (V.conj().T @ to_dense(rho0) @ V).flatten()
+        es = [(V.conj().T @ to_dense(e) @ V).flatten() for e in e_ops]
+        dev = self._Rdev.device
+        Ud = torch.from_numpy(np.ascontiguousarray(self.U)).to(dev)                  # (M, M, T)
+        rho = torch.einsum('abk,b->ak', Ud, torch.from_numpy(r0).to(dev))          # (M, T)
+        E = torch.from_numpy(np.stack(es) if es else np.zeros((0, r0.size), complex)).to(dev)
+        return (E @ rho).T.cpu().numpy()
+
+    def correlation_2op_1t(self, rho0, a, b, tau):
+        """<<1| a G(tau) b |rho0>> for Liouville-space operators a, b (M x M)."""
+        if self.G is None:
+            self.propagator(tau)
+        dev = self._Rdev.device
+        den = lambda x: torch.from_numpy(np.ascontiguousarray(to_dense(x), dtype=complex)).to(dev)  # noqa: E731
+        r0 = to_dense(rho0)
+        r0 = r0.flatten() if r0.ndim == 2 else r0
+        G = torch.from_numpy(np.ascontiguousarray(self.G)).to(dev)
+        v = den(b) @ torch.from_numpy(np.asarray(r0, dtype=complex)).to(dev)
+        tmp = den(a) @ torch.einsum('abk,b->ak', G, v)                               # (M, T)
+        idm = torch.from_numpy(np.eye(self.dim).flatten().astype(complex)).to(dev)
+        return (idm @ tmp).cpu().numpy()
+
+    def correlation_4op_3t(self, rho0, oplist, signature, tau):
+        """<<1| A G(tau3) B G(tau2) C G(tau1) D |rho0>> as (tau3, tau2, tau1)
+        (``pyqed/oqs.py:239-330``); the operators act as the superoperators
+        ``signature`` names ('l', 'r', 'c', 'a'), all in the eigenbasis.  Uses
+        the stored G when there is one, as the reference."""
+        if len(oplist) != 4:
+            raise ValueError('Number of operators is not 4.')
+        sup = [_superop(to_dense(o), sgn) for o, sgn in zip(oplist, signature)]
+        if self.G is None:
+            self.propagator(tau)
+        dev = self._Rdev.device
+        tt = lambda x: torch.from_numpy(np.ascontiguousarray(x, dtype=complex)).to(dev)  # noqa: E731
+        G = tt(self.G)
+        a, b, c, d = (tt(x) for x in sup)
+        rho = d @ tt(to_dense(rho0).flatten())
+        tmp = torch.einsum('abk,b->ak', G, rho)
+        tmp = c @ tmp
+        tmp = torch.einsum('abj,bk->ajk', G, tmp)
+        tmp = torch.einsum('ab,bjk->ajk', b, tmp)
+        tmp = torch.einsum('abi,bjk->aijk', G, tmp)
+        idm = tt(np.eye(self.dim).flatten())
+        return torch.einsum('a,ab,bijk->ijk', idm, a, tmp).cpu().numpy()
+
+    def steady_state(self):
+        """The null vector of R (eigenvalue of smallest modulus), normalised
+        to unit trace, as a density matrix in the original basis."""
+        if self.R is None:
+            self.redfield_tensor()
+        evals, vecs = scipy.linalg.eig(self.R.toarray())
+        v = vecs[:, np.argmin(np.abs(evals))].reshape(self.dim, self.dim)
+        v = v / np.trace(v)
+        return self.evecs @ v @ self.evecs.conj().T
 
     def evolve(self, rho0, dt, Nt, evecs=None, e_ops=[], store_states=False, t0=0, nout=1, *,
                precision="fp64"):
@@ -215,6 +343,22 @@ class RedfieldSolver:
         else:
             result.rholist = []
         return result
+
+
+def _superop(a, kind):
+    """Row-major superoperator of ``a`` (``operator_to_superoperator``,
+    ``pyqed/superoperator.py:200-246``)."""
+    n = a.shape[-1]
+    i = np.eye(n)
+    if kind in ['commutator', 'c', '-']:
+        return np.kron(a, i) - np.kron(i, a.T)
+    if kind in ['left', 'l']:
+        return np.kron(a, i)
+    if kind in ['right', 'r']:
+        return np.kron(i, a.T)
+    if kind in ['anticommutator', 'a', '+']:
+        return np.kron(a, i) + np.kron(i, a.T)
+    raise ValueError('Error: superoperator {} does not exist.'.format(kind))
 
 
 def redfield_batch(H, a_ops, spectra, rho0, dt, Nt, e_ops=None, *, precision="fp32", store_every=0,

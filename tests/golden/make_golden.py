@@ -88,6 +88,26 @@ def redfield_fixtures(oqs):
         rho0=rho0, e_ops=np.stack([H, a_ops[0]]), dt=0.05, nt=120, R=sol.R.toarray(), evecs=sol.evecs,
         observables=r.observables, rho_last=r.rholist[-1])
 
+    # the Liouville-space propagator, expectation values, Green's function and
+    # 4-point correlation of a 3-site chain (pyqed/oqs.py:136-330)
+    import contextlib
+    import io
+    ch = W.redfield_chain(n=3, seed=5)
+    t = np.linspace(0.0, 2.0, 6)
+    ops = [ch["e_ops"][0], ch["a_ops"][1], ch["a_ops"][0], ch["e_ops"][1]]
+    with contextlib.redirect_stdout(io.StringIO()):
+        sol = oqs.RedfieldSolver(ch["H"], c_ops=ch["a_ops"], spectra=ch["spectra"])
+        R, V = sol.redfield_tensor()
+        sol.evecs = V
+        U_sos = sol.propagator(t)
+        ex = sol.expect(ch["rho0"], ch["e_ops"])
+        c4 = sol.correlation_4op_3t(ch["rho0"], ops, "llrr", t[:4])
+        G = sol.gf(t, method="diag")
+        sol2 = oqs.RedfieldSolver(ch["H"], c_ops=ch["a_ops"], spectra=ch["spectra"])
+        sol2.redfield_tensor()
+        U_eom = sol2.propagator(t, method="EOM")
+    out["redfield_aux"] = dict(t=t, R=R.toarray(), evecs=V, U_sos=U_sos, U_eom=U_eom, expect=ex, c4=c4, gf=G,
+                               ops=np.stack(ops), rho0=ch["rho0"])
     return out
 
 

@@ -102,3 +102,44 @@ def test_redfield_batched_tensor_build_matches_single():
         R1 = build_tensor(p[0], p[2], p[3]).cpu().numpy()
         assert np.array_equal(Rb[off:off + n ** 4], R1)
         off += n ** 4
+
+
+def test_redfield_solver_propagator_expect_gf_c4_golden(golden):
+    g = golden("redfield_aux")
+    ch = W.redfield_chain(n=3, seed=5)
+    sol = RedfieldSolver(ch["H"], c_ops=ch["a_ops"], spectra=ch["spectra"])
+    R, V = sol.redfield_tensor()
+    t = g["t"]
+    U = sol.propagator(t)
+    assert U.shape == g["U_sos"].shape and np.abs(U - g["U_sos"]).max() < 1e-10
+    assert np.abs(sol.expect(ch["rho0"], ch["e_ops"]) - g["expect"]).max() < 1e-10
+    # the stored G is used, whatever tau is given (as the reference)
+    c4 = sol.correlation_4op_3t(ch["rho0"], list(g["ops"]), "llrr", t[:4])
+    assert c4.shape == g["c4"].shape and np.abs(c4 - g["c4"]).max() < 1e-10
+    assert np.abs(sol.gf(t, method="diag") - g["gf"]).max() < 1e-10
+    sol2 = RedfieldSolver(ch["H"], c_ops=ch["a_ops"], spectra=ch["spectra"])
+    sol2.redfield_tensor()
+    U2 = sol2.propagator(t, method="EOM")
+    assert np.abs(U2 - g["U_eom"]).max() < 1e-12
+    assert np.abs(sol2.gf(t) + 1j * g["U_eom"]).max() < 1e-12
+
+
+def test_redfield_solver_correlation_2op_and_steady_state():
+    from oracle import redfield_oracle as RO
+    ch = W.redfield_chain(n=4, seed=6)
+    sol = RedfieldSolver(ch["H"], c_ops=ch["a_ops"], spectra=ch["spectra"])
+    R, V = sol.redfield_tensor()
+    M = 16
+    tau = np.linspace(0.0, 3.0, 7)
+    a = RO.superop(ch["e_ops"][0], "l")
+    b = RO.superop(ch["a_ops"][1], "l")
+    r0 = V.conj().T @ ch["rho0"] @ V
+    c = sol.correlation_2op_1t(r0, a, b, tau)
+    G = -1j * RO.propagator_sos(R.toarray(), tau)
+    ref = np.eye(4).flatten() @ (a @ np.tensordot(G, b @ r0.flatten(), axes=([1], [0])))
+    assert c.shape == (7,) and np.abs(c - ref).max() < 1e-10
+    rss = sol.steady_state()
+    assert abs(np.trace(rss) - 1) < 1e-10
+    v = (V.conj().T @ rss @ V).flatten()
+    assert np.abs(R.toarray() @ v).max() < 1e-10
+    del M

@@ -226,3 +226,21 @@ def test_spectral_oracle_matches_reference(golden):
     assert c32.shape == (len(tau), len(tl)) and np.abs(c32 - g["c3_2t"]).max() < 1e-10
     c42 = SO.correlation_3op_2t(eig, g["rho0"], a, b @ c, d, tl, tau)
     assert np.abs(c42 - g["c4_2t"]).max() < 1e-10
+
+
+def test_redfield_aux_oracle_matches_reference(golden):
+    """Propagator ('SOS' and RK4 'EOM'), expect, Green's function and the
+    4-point correlation of RedfieldSolver (pyqed/oqs.py:136-330)."""
+    from oracle import redfield_oracle as RO
+    g = golden("redfield_aux")
+    ch = W.redfield_chain(n=3, seed=5)
+    R, V = RO.redfield_tensor(ch["H"], ch["a_ops"], ch["spectra"])
+    assert np.abs(R - g["R"]).max() < 1e-12
+    t = g["t"]
+    U = RO.propagator_sos(R, t)
+    assert np.abs(U - g["U_sos"]).max() < 1e-10
+    assert np.abs(RO.propagator_eom(R, t) - g["U_eom"]).max() < 1e-12
+    assert np.abs(RO.expect(U, ch["rho0"], V, ch["e_ops"]) - g["expect"]).max() < 1e-10
+    assert np.abs(-1j * U - g["gf"]).max() < 1e-10
+    c4 = RO.correlation_4op_3t(-1j * U, ch["rho0"], list(g["ops"]), "llrr")
+    assert c4.shape == g["c4"].shape and np.abs(c4 - g["c4"]).max() < 1e-10
