@@ -26,6 +26,8 @@ inputs) and the outputs of the reference's own entry points:
 * ``spectral_jc.npz`` the eigen-decomposition ``Lindblad_solver``
                      (``pyqed/superoperator.py:455-770``) correlations on
                      the Jaynes-Cummings system with 3 Fock states.
+* ``api_signatures.json`` the public methods and parameter names of the
+                     reference classes the mirrors replace.
 * ``heom_*.npz``     ``HEOMSolver.run`` (``_heom``) on the reference's
                      spin-boson example and a 6-site chain, and
                      ``HEOMSolver.propagator`` (``_heom_propagator``) on a
@@ -172,6 +174,26 @@ def spectral_fixtures():
         c4_2t=sol.correlation_4op_2t(rho0, [a, b, c, d], tl, tau))}
 
 
+def api_fixture():
+    """Public method names and parameter names of the reference classes the
+    mirrors replace (a drop-in must accept the same calls)."""
+    import importlib
+    import inspect
+    import json
+    oqs = load()
+    so = importlib.import_module("pyqed.superoperator")
+    api = {}
+    for key, cls in (("LindbladSolver", oqs.LindbladSolver), ("RedfieldSolver", oqs.RedfieldSolver),
+                     ("HEOMSolver", oqs.HEOMSolver), ("Lindblad_solver", so.Lindblad_solver)):
+        api[key] = {name: [p.name for p in inspect.signature(f).parameters.values()]
+                    for name, f in inspect.getmembers(cls, inspect.isfunction)
+                    if not name.startswith("_") or name == "__init__"}
+    path = os.path.join(HERE, "api_signatures.json")
+    with open(path, "w") as f:
+        json.dump(api, f, indent=1, sort_keys=True)
+    print("api_signatures", os.path.getsize(path), "bytes")
+
+
 def main():
     oqs = load()
     out = {}
@@ -271,6 +293,7 @@ def main():
     out.update(heom_fixtures(oqs))
     out.update(spectral_fixtures())
     save(out)
+    api_fixture()
 
 
 def save(out):
@@ -287,5 +310,7 @@ if __name__ == "__main__":
         save(heom_fixtures(load()))
     elif sys.argv[1:] == ["spectral"]:
         save(spectral_fixtures())
+    elif sys.argv[1:] == ["api"]:
+        api_fixture()
     else:
         main()
