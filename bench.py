@@ -266,6 +266,8 @@ def run_gpu(args):
             traffic = int(reads * (23.10 / 24.30)) + writes
         line["roofline"] = dict(bound="tensor", achieved=achieved, peak=pk, unit="TFLOP/s",
                                 frac=achieved / pk, traffic=traffic,
+                                # the split product runs three MMA products per algorithmic one
+                                executed=3.0 * achieved, executed_frac=3.0 * achieved / pk,
                                 traffic_note="bytes per launch: ncu-measured reads scaled to the "
                                              "full batch + algorithmic writes (profiles/)",
                                 note="algorithmic 64*N^3 flops per instance-step; peak = "
