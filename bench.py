@@ -475,6 +475,38 @@ def measure_redfield(args, dev, n_inst=2048, n=8, nt=1000, dt=0.1):
     return out
 
 
+def measure_size_class(args, dev, N=65, n_inst=152, nt=400, dt=0.05):
+    """One size class of the exciton family alone: n_inst instances of
+    dimension N (exciton_instance(N - 1, i, seed=5), dephasing on every site,
+    the transition dipole as the observable), 3xTF32, nt RK4 steps.  Reports
+    the per-instance-step time and the cycles per RK4 stage at 2.07 GHz; with
+    n_inst = 152 every SM holds one instance, so this is the per-stage cost
+    of that size's tensor-core kernel (N = 65 runs the border kernel)."""
+    import torch
+    from pyqed_gb300 import workloads as W
+    from pyqed_gb300.batch import prepare_batch
+    from pyqed_gb300.engine import Propagator
+    insts = [W.exciton_instance(N - 1, index=i, seed=5) for i in range(n_inst)]
+    bi = prepare_batch([x["H"] for x in insts], [[np.diag(c) for c in x["c_diag"]] for x in insts],
+                       [x["rho_g"] for x in insts], [[x["mu"]] for x in insts])
+    prop = Propagator(bi.dims, nt=nt, dt=dt, n_cops=bi.n_cops, cops_kind=bi.cops_kind, n_eops=1,
+                      precision=args.precision)
+    prop.set_operators(bi.H, bi.cops, bi.eops, bi.dops)
+    r0 = prop.to_device(bi.rho0)
+    o = prop.alloc_outputs(want_obs=True, want_rho=False)
+    prop.propagate_device(r0, None, o)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    prop.propagate_device(r0, None, o)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    prop.close()
+    return dict(workload="exciton N=%d x %d" % (N, n_inst), N=N, n_inst=n_inst, nt=nt, precision=args.precision,
+                ms=ms, us_per_step=ms * 1e3 / nt, cycles_per_stage_at_2070mhz=ms * 1e-3 / nt / 4 * 2.07e9)
+
+
 def heom_flops(N, nado, diag_sz=False):
     """Algorithmic flops of one sweep (one instance-step): level 0 and level
     nado-2 take two commutators (4 complex N^3 products), the levels between
@@ -766,6 +798,13 @@ def main():
     ap.add_argument("--only-heom", action="store_true", help="run only the batched HEOM section")
     ap.add_argument("--heom-n-inst", type=int, default=4096)
     ap.add_argument("--heom-nt", type=int, default=1000)
+    ap.add_argument("--only-redfield", action="store_true", help="run only the batched Redfield section")
+    ap.add_argument("--rf-n-inst", type=int, default=2048)
+    ap.add_argument("--rf-nt", type=int, default=1000)
+    ap.add_argument("--only-size-class", type=int, default=None, metavar="N",
+                    help="time one size class of the exciton family alone (N = 65: the border kernel)")
+    ap.add_argument("--class-n-inst", type=int, default=152)
+    ap.add_argument("--class-nt", type=int, default=400)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -782,6 +821,20 @@ def main():
         build()
         print(json.dumps(dict(heom=measure_heom(args, torch.device("cuda", 0), n_inst=args.heom_n_inst,
                                                 nt=args.heom_nt))))
+        return
+    if args.only_redfield:
+        import torch
+        from pyqed_gb300.build import build
+        build()
+        print(json.dumps(dict(redfield=measure_redfield(args, torch.device("cuda", 0), n_inst=args.rf_n_inst,
+                                                        nt=args.rf_nt))))
+        return
+    if args.only_size_class is not None:
+        import torch
+        from pyqed_gb300.build import build
+        build()
+        print(json.dumps(dict(size_class=measure_size_class(args, torch.device("cuda", 0), N=args.only_size_class,
+                                                            n_inst=args.class_n_inst, nt=args.class_nt))))
         return
     if args.only_adjoint:
         import torch
