@@ -147,6 +147,8 @@ def run_gpu(args):
     n_inst = int(bi.dims.size)
     chosen = args.precision
     paths = [chosen] + ([] if args.no_plain or chosen == "fp32" else ["fp32"])
+    if chosen == "3xbf16" and not args.no_plain:
+        paths.append("3xtf32")  # the other split precision, timed and checked beside it
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     drive_shared = wl["drive"] is None or wl["drive"].ndim == 2
@@ -285,6 +287,13 @@ def run_gpu(args):
         pl = results["fp32"]
         line["plain"] = dict(value=inst_steps / pl["sec_per_step"], ms_per_step=pl["sec_per_step"] * 1e3,
                              speedup_chosen_over_plain=pl["sec_per_step"] / ch["sec_per_step"])
+    for alt in results:
+        if alt not in (chosen, "fp32"):
+            a = results[alt]
+            line.setdefault("alternatives", {})[alt] = dict(
+                value=inst_steps / a["sec_per_step"], ms_per_step=a["sec_per_step"] * 1e3,
+                speedup_over_plain=(results["fp32"]["sec_per_step"] / a["sec_per_step"]
+                                    if "fp32" in results else None))
     line["e2e"] = dict(value=inst_steps / e2e_t, unit=UNIT, ms_per_step=e2e_t * 1e3,
                        h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
                        api="pyqed_gb300.engine.Propagator.set_operators + propagate "
@@ -771,7 +780,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="exciton4096")
-    ap.add_argument("--precision", default=os.environ.get("LGB_BENCH_PRECISION", "3xtf32"))
+    ap.add_argument("--precision", default=os.environ.get("LGB_BENCH_PRECISION", "3xbf16"))
     ap.add_argument("--n-inst", type=int, default=None)
     ap.add_argument("--nt", type=int, default=None)
     ap.add_argument("--no-plain", action="store_true")

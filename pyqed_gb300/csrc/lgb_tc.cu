@@ -29,6 +29,13 @@
 // and the stage input in registers, performs the RK4 stage combination
 // (pyqed/phys.py:1051-1064) with a Kahan-compensated final update, splits the
 // next stage input into hi/lo and writes it into the XM and X^T buffers.
+// With BF16 operands the diagonal of A stays out of the split products: its
+// entries are of order one (the site energies) and BF16 hi + lo holds them
+// only to ~2^-17 relative, which turns into a phase error growing with t.
+// Its term (a_i + conj(a_j)) X_ij is formed in FP32 from the FP32 stage input
+// and written into the part-0 accumulator columns (part-1 columns zeroed)
+// before the stage's MMAs, which accumulate onto it; the off-diagonal
+// couplings are small, so their BF16 representation error is too.
 // Observables Tr[O rho] (pyqed/phys.py:1257-1264) of step k are reduced while
 // the tensor core runs the first stage of step k + 1.  Every mbarrier wait is
 // bounded; a wait that runs out marks the instance LGB_ERR_TIMEOUT and the CTA
@@ -79,6 +86,7 @@ template <> struct Elem<true> {
 // Two thread groups (the warps of TMEM lane quarters 0-1 and 2-3) run separate
 // instances when NP <= 32; otherwise group 0 is the whole CTA.
 struct TcShared {
+  alignas(16) float2 adg[2][64];  // BF16: diagonal of A of each group's instance
   uint64_t mbar[2];
   uint32_t tmem_base;
   int next[2];
@@ -187,9 +195,10 @@ __device__ __forceinline__ void issue_stage(uint32_t d, uint32_t base, uint32_t 
   const uint64_t dXM = sdesc(base + G::OFF_XM - mshift, 128, G::SBO_S);
   const uint64_t dXT = sdesc(base + G::OFF_XT, G::LBO_T, G::SBO_T);
   // A X: A_hi X_hi, A_hi X_lo, A_lo X_hi
+  // (BF16: the accumulator already holds the diagonal term, so every MMA accumulates)
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, s > 0 ? 1u : 0u);
+    mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, (BF16 || s > 0) ? 1u : 0u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
     mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, G::LVL_T + s * G::KSTEP_T), id, 1u);
@@ -320,6 +329,12 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
             a.y = fmaf(f[d], g.y, a.y);
           }
       }
+      if constexpr (BF16) {
+        if (k == r) {  // applied in FP32 by inject
+          sh.adg[grp][r] = a;
+          a = make_float2(0.f, 0.f);
+        }
+      }
       float h, lo;
       El::split(a.x, h, lo);
       *reinterpret_cast<ET*>(SA + off_s<BF16, NP>(mrow(0, r), k)) = (ET)h;
@@ -352,6 +367,35 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     }
     st4<BF16>(SXM + off_s<BF16, NP>(xm_row, col), vh);
     st4<BF16>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col), vl);
+  };
+  // BF16: the diagonal term (a_i + conj(a_j)) X_ij of the stage input x
+  // (columns j0 + 4g .. + 3; the partner lane holds the other component) into
+  // the part-0 accumulator columns, the part-1 columns zeroed.  Warp-uniform.
+  const float sgx = c == 0 ? -1.f : 1.f;
+  // ai: a_i of this thread's row (adg_row())
+  auto adg_row = [&]() -> float2 { return row_ok ? sh.adg[grp][i] : make_float2(0.f, 0.f); };
+  auto inject = [&](int g, const float* x4, float2 ai) {
+    if constexpr (BF16) {
+      const int col = j0 + g * 4;
+      float q[4];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float4 aj = *reinterpret_cast<const float4*>(&sh.adg[grp][col + 2 * h]);
+        const float2 x2 = make_float2(x4[2 * h], x4[2 * h + 1]);
+        const float2 xp2 = make_float2(__shfl_xor_sync(0xffffffffu, x4[2 * h], 16),
+                                       __shfl_xor_sync(0xffffffffu, x4[2 * h + 1], 16));
+        // Re: (ar_i + ar_j) xr - (ai_i - ai_j) xi,  Im: (ar_i + ar_j) xi + (ai_i - ai_j) xr
+        const float2 dx2 = __fadd2_rn(make_float2(ai.x, ai.x), make_float2(aj.x, aj.z));
+        const float2 sdy2 = __ffma2_rn(make_float2(-sgx, -sgx), make_float2(aj.y, aj.w),
+                                       make_float2(sgx * ai.y, sgx * ai.y));
+        const float2 q2 = __ffma2_rn(sdy2, xp2, __fmul2_rn(dx2, x2));
+        q[2 * h] = q2.x;
+        q[2 * h + 1] = q2.y;
+      }
+      const float z[4] = {0.f, 0.f, 0.f, 0.f};
+      tmem_st4(tlane + (uint32_t)ncol(0, col), q);
+      tmem_st4(tlane + (uint32_t)ncol(1, col), z);
+    }
   };
   // hi + lo of the current stage input of group g, read back from XM (used by
   // the general diagonal dissipator)
@@ -713,6 +757,20 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       for (int d = 0; d < 4; ++d) f[d] = (d < p.n_drive) ? (float)drv[(long long)d * p.nt + step] : 0.f;
       build_a(f);
     }
+    if constexpr (BF16) {
+      // diagonal term of the first stage (later steps of a static H get it from
+      // the last epilogue of the step before)
+      if (step == 0 || p.n_drive > 0) {
+        gsync<GR>(grp);  // the diagonal written by build_a
+        const float2 ai = adg_row();
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          const float x4[4] = {rho2[2 * g].x, rho2[2 * g].y, rho2[2 * g + 1].x, rho2[2 * g + 1].y};
+          inject(g, x4, ai);
+        }
+        tmem_wait_st();
+      }
+    }
 #pragma unroll 1
     for (int stage = 0; stage < 4; ++stage) {
       sync_for_mma<GR>(grp);
@@ -756,6 +814,8 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         // (M conj(b))_i partial of the next stage input
         [[maybe_unused]] float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f, tx = 0.f, ty = 0.f;
         [[maybe_unused]] const float2* brow = nullptr;
+        [[maybe_unused]] float2 ai_row = make_float2(0.f, 0.f);
+        if constexpr (BF16) ai_row = adg_row();
         if constexpr (BD) {
           const float2 ai = bd->aB[i], ci = bd->bx[bcur][0][i];
           u0 = c == 0 ? ai.x : ai.y;
@@ -832,7 +892,11 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
           }
           const float x4[4] = {xn2[0].x, xn2[0].y, xn2[1].x, xn2[1].y};
           write_group(g, x4);
+          if constexpr (BF16) {
+            if (STAGE < 3 || p.n_drive == 0) inject(g, x4, ai_row);
+          }
         }
+        if constexpr (BF16) tmem_wait_st();
         if constexpr (BD) {
           tx += __shfl_xor_sync(0xffffffffu, tx, 16);
           ty += __shfl_xor_sync(0xffffffffu, ty, 16);

@@ -156,6 +156,19 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// ---- registers -> TMEM (32 lanes x 32 bit per warp) --------------------------------
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])));
+}
+// (orders every earlier tcgen05.st of the thread; the stores themselves carry
+// no compiler memory clobber, so that the surrounding code can be scheduled
+// across them)
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 // ---- split-precision helpers ---------------------------------------------------------------
 // Round an FP32 value to TF32 (nearest, ties away from zero); the result is an
 // FP32 bit pattern with the 13 low mantissa bits clear.

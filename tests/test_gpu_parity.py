@@ -180,7 +180,10 @@ def test_correlation_two_time_intended_semantics():
 
 # ---- split-precision tensor-core path --------------------------------------------
 
-@pytest.mark.parametrize("prec,tol", [("3xtf32", TOL32), ("3xbf16", 1e-3)])
+# 3xBF16 keeps the diagonal of A out of the split products (applied in FP32),
+# so on the exciton family (couplings small beside the energy spread) it meets
+# the FP32 bar; on dense GUE Hamiltonians it keeps the looser TOLBF.
+@pytest.mark.parametrize("prec,tol", [("3xtf32", TOL32), ("3xbf16", TOL32)])
 def test_split_exciton_golden(golden, prec, tol):
     g = golden("exciton")
     ex = W.exciton_batch(indices=[int(i) for i in g["indices"]], nt=int(g["nt"]))
@@ -192,7 +195,7 @@ def test_split_exciton_golden(golden, prec, tol):
     assert err < tol, err
 
 
-@pytest.mark.parametrize("prec,tol", [("3xtf32", TOL32), ("3xbf16", 1e-3)])
+@pytest.mark.parametrize("prec,tol", [("3xtf32", TOL32), ("3xbf16", TOL32)])
 def test_split_uneven_batch_vs_oracle(prec, tol):
     # every padded size class of the tensor-core kernel (16/32/48/64) plus N=65
     idx = list(range(40))
@@ -277,7 +280,10 @@ def test_split_border_driven_n65_takes_the_fp32_kernel():
         assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < TOL32 * 10
 
 
-def test_split_driven_diag_vs_oracle():
+@pytest.mark.parametrize("prec,tol", [("3xtf32", TOL32), ("3xbf16", TOLBF)])
+def test_split_driven_diag_vs_oracle(prec, tol):
+    """Driven H(t): the A operand (and, for BF16, its diagonal kept in FP32)
+    is rebuilt every step."""
     rng = np.random.default_rng(22)
     dims = [8, 33, 64]
     E = W.gp_pulse(15, 0.02, seed=9, amp=0.3)
@@ -290,12 +296,12 @@ def test_split_driven_diag_vs_oracle():
         psi /= np.linalg.norm(psi)
         rho0.append(np.outer(psi, psi.conj()))
     res = propagate_batch(H0, cops, rho0, 0.02, 15, e_ops=[[m] for m in mu], obs_t0=False,
-                          precision="3xtf32", drive_ops=[[m] for m in mu], drive=E[None, :])
+                          precision=prec, drive_ops=[[m] for m in mu], drive=E[None, :])
     for b in range(len(dims)):
         obs, states = O.lindblad_driven([H0[b], [mu[b], E]], rho0[b], cops[b], [mu[b]],
                                         Nt=15, dt=0.02)
-        assert np.abs(res["rho"][b] - states[-1]).max() < TOL32
-        assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < TOL32 * 10
+        assert np.abs(res["rho"][b] - states[-1]).max() < tol
+        assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < tol * 10
 
 
 def test_split_solver_run_matches_fp64():
