@@ -266,6 +266,18 @@ __device__ __forceinline__ void st4(unsigned char* base, const float* v) {
   }
 }
 
+// Store 8 consecutive K elements of one BF16 operand row (a, then b; 16 bytes).
+__device__ __forceinline__ void st8_bf16(unsigned char* base, const float* a, const float* b) {
+  const __nv_bfloat162 p0 = __floats2bfloat162_rn(a[0], a[1]), p1 = __floats2bfloat162_rn(a[2], a[3]);
+  const __nv_bfloat162 p2 = __floats2bfloat162_rn(b[0], b[1]), p3 = __floats2bfloat162_rn(b[2], b[3]);
+  uint4 u;
+  u.x = *reinterpret_cast<const uint32_t*>(&p0);
+  u.y = *reinterpret_cast<const uint32_t*>(&p1);
+  u.z = *reinterpret_cast<const uint32_t*>(&p2);
+  u.w = *reinterpret_cast<const uint32_t*>(&p3);
+  *reinterpret_cast<uint4*>(base) = u;
+}
+
 // One instance, all Nt steps.  Thread mapping: warp w reads TMEM lane quarter
 // q = w & 3 and owns columns [(w >> 2) NP/4, (w >> 2 + 1) NP/4) of its lane;
 // lane l of the warp is TMEM lane 32 q + l = M row (c, i) with c = l >> 4,
@@ -351,6 +363,12 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   // written 4 columns at a time (group g: columns j0 + 4g .. j0 + 4g + 3).
   const int xm_row = mrow(1 - c, i);
   const float xm_sign = c == 0 ? -1.f : 1.f;
+  // BF16 with a multiple of 8 columns per thread: the XM values of an even
+  // group wait for the odd one and both go out as one 16-byte store per level
+  // (8-byte stores of the 32 rows of a warp, 1 KB apart per row group, would
+  // share one bank set).  Every caller walks the groups in order.
+  constexpr bool kXmPairs = BF16 && (NPQ % 8 == 0);
+  [[maybe_unused]] float xmh[4], xml[4];
   auto write_group = [&](int g, const float* x4) {
     if (!row_ok) return;
     float vh[4], vl[4];
@@ -365,8 +383,21 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       vh[e] *= xm_sign;
       vl[e] *= xm_sign;
     }
-    st4<BF16>(SXM + off_s<BF16, NP>(xm_row, col), vh);
-    st4<BF16>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col), vl);
+    if constexpr (kXmPairs) {
+      if ((g & 1) == 0) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          xmh[e] = vh[e];
+          xml[e] = vl[e];
+        }
+      } else {
+        st8_bf16(SXM + off_s<BF16, NP>(xm_row, col - 4), xmh, vh);
+        st8_bf16(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col - 4), xml, vl);
+      }
+    } else {
+      st4<BF16>(SXM + off_s<BF16, NP>(xm_row, col), vh);
+      st4<BF16>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col), vl);
+    }
   };
   // BF16: the diagonal term (a_i + conj(a_j)) X_ij of the stage input x
   // (columns j0 + 4g .. + 3; the partner lane holds the other component) into
