@@ -10,12 +10,15 @@ propagation of the batch (4096 x 4000 instance-steps).
   python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload exciton4096|driven256|jc16] [--n-inst N] [--nt T]
 
-Prints one JSON line.  ``value`` is the chosen path with inputs resident in
+Prints one JSON line.  ``value`` is the chosen path (``--precision``, by
+default 3xBF16 with the diagonal of A applied in FP32) with inputs resident in
 HBM (device-timed with CUDA events on the launch stream, L2 flushed between
 steps); ``e2e`` times the public batched API including the host->device copy
 of every input from pinned memory and the device->host read of C(t).
-``plain`` is the FP32 CUDA-core path on the same inputs; ``cpu_baseline`` is
-the oracle port of the reference's dense algorithm on the host cores.
+``plain`` is the FP32 CUDA-core path on the same inputs, ``alternatives``
+the 3xTF32 path; ``accuracy`` checks each against the complex128 oracle;
+``cpu_baseline`` is the oracle port of the reference's dense algorithm on the
+host cores.
 """
 from __future__ import annotations
 
