@@ -6,7 +6,7 @@
  * (pyqed/oqs.py:1114-1330).  Each entry point below replaces one piece of
  * that class's call stack; the Python mirror pyqed_gb300.oqs.LindbladSolver
  * binds them with ctypes exactly as a maintainer of the reference would
- * (INTEGRATION.md shows the binding).
+ * (pyqed_gb300/_capi.py is that binding).
  *
  * Conventions
  *  - All matrices are complex128, interleaved (re, im) doubles, row-major.
@@ -332,8 +332,8 @@ int lgb_spectral_2t(int32_t k, int32_t n_tau, int32_t n_t, const double* lambda,
  *
  * For callers that cannot call cudaMalloc -- a process whose device memory
  * was handed to another allocator up front (a framework's caching allocator,
- * a fixed arena in a serving process), or code issuing work while a stream
- * is being captured into a CUDA graph, where allocation is not allowed.
+ * a fixed arena in a serving process), or an embedding whose device-memory
+ * budget is fixed before this library is loaded.
  * It propagates ONE instance in complex128 (the same FP64 kernel as
  * lgb_plan_propagate with LGB_PREC_FP64) and keeps every working buffer in a
  * fixed array compiled into the library (about 1.1 MB, held on every device
@@ -351,7 +351,8 @@ int lgb_spectral_2t(int32_t k, int32_t n_tau, int32_t n_t, const double* lambda,
  * Limits: N <= LGB_NOALLOC_MAX_DIM, n_cops <= LGB_NOALLOC_MAX_COPS,
  * n_eops <= LGB_NOALLOC_MAX_EOPS; larger requests return LGB_ERR_TOO_LARGE.
  * The first call on a device looks up the array's device address (once per
- * device); make that first call before any stream capture begins.  All calls
+ * device and context: again after a reset of the device); make that first
+ * call before any stream capture begins.  All calls
  * share the one array, so calls that overlap on the GPU (different streams,
  * or different host threads on the same device) race: serialise them.
  * Asynchronous on `stream`. */

@@ -2,20 +2,23 @@
 //
 // Some callers cannot call cudaMalloc: a process whose device heap was
 // handed to another allocator at start-up (a framework's caching allocator
-// or a fixed arena in a serving process), or code that issues work while a
-// stream is being captured into a CUDA graph, where allocation is not
-// permitted.  For them this entry point runs the FP64 CTA-resident kernel
-// (the check path of lgb_plan_propagate) with every piece of working memory
-// -- the prepared operators, the RK4 state slabs, the dense-collapse
-// scratch and the small per-instance tables -- placed in one file-scope
-// __device__ array of fixed size.  The caller still passes its inputs and
-// outputs as device pointers.
+// or a fixed arena in a serving process), or an embedding whose memory
+// budget is fixed before this library is loaded.  For them this entry point
+// runs the FP64 CTA-resident kernel (the check path of lgb_plan_propagate)
+// with every piece of working memory -- the prepared operators, the RK4
+// state slabs, the dense-collapse scratch and the small per-instance tables
+// -- placed in one file-scope __device__ array of fixed size.  The caller
+// still passes its inputs and outputs as device pointers.
 //
 // The array lives as long as the library is loaded, on every device that
-// loads it.  Its device address is looked up once per device (the first call
-// on that device, which therefore should come before any stream capture).
-// Every call reuses the same array: concurrent calls on different streams of
-// the same device race and must be serialised by the caller.
+// loads it.  Its device address is looked up once per device and CUDA
+// context (the first call on that device, which therefore should come
+// before any stream capture; a call after the device's context was reset
+// looks it up again).  Every call reuses the same array: concurrent calls on
+// different streams of the same device race and must be serialised by the
+// caller.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "lgb_internal.h"
@@ -37,10 +40,41 @@ static __device__ __align__(256) unsigned char g_lgb_noalloc_scratch[kScratchByt
 
 struct DevScratch {
   unsigned char* base = nullptr;
+  unsigned long long ctx_id = 0;  // the context the address belongs to
   bool ready = false;
 };
 DevScratch g_dev[64];
 std::mutex g_mu;
+
+// ID of the current CUDA context (0 if the driver cannot tell).  The
+// runtime is linked statically and the driver library is not linked, so
+// the two driver calls are looked up through the runtime.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    cudaGetLastError();
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current == nullptr || get_id == nullptr || get_current(&ctx) != CUDA_SUCCESS ||
+      ctx == nullptr || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 // Small per-instance tables (one instance) written by a kernel from its
 // arguments, so that no host-to-device copy is needed.
@@ -58,14 +92,20 @@ __global__ void noalloc_tables_kernel(Tables* t, int N, int NP, unsigned char pl
   t->err = 0;
   t->off = t->doff = t->woff = t->soff = 0;
   t->place = place;
-  t->shift = 0.0;
+  t->shift = 0.0;  // overwritten by the trace-shift kernel of launch_setup (Re Tr(H) / N)
 }
 
 int scratch_for_current_device(unsigned char** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return LGB_ERR_CUDA;
   if (dev < 0 || dev >= 64) return LGB_ERR_UNSUPPORTED;
+  // (the caller's device pointers imply that the device's context exists;
+  // if the driver cannot name it, the address is looked up on every call)
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_mu);
+  // a reset of the device (cudaDeviceReset) unloads the module: the address
+  // belongs to the context it was looked up in
+  if (g_dev[dev].ready && (ctx == 0 || g_dev[dev].ctx_id != ctx)) g_dev[dev].ready = false;
   if (!g_dev[dev].ready) {
     void* p = nullptr;
     // the array's name is a host-side stand-in: its device address must be
@@ -75,6 +115,7 @@ int scratch_for_current_device(unsigned char** out) {
       return LGB_ERR_CUDA;
     }
     g_dev[dev].base = static_cast<unsigned char*>(p);
+    g_dev[dev].ctx_id = ctx != 0 ? ctx : current_context_id();
     g_dev[dev].ready = true;
   }
   *out = g_dev[dev].base;

@@ -1,9 +1,13 @@
 """Generate the golden fixtures from the reference implementation itself.
 
-Run in a container where the reference (binggu56/pyqed 0.1.3) is mounted at
-``/root/reference``:
+Run in a container where the reference (binggu56/pyqed 0.1.3) is mounted,
+with ``PYQED_REFERENCE`` set to its directory:
 
-    python tests/golden/make_golden.py
+    PYQED_REFERENCE=/root/reference python tests/golden/make_golden.py
+    PYQED_REFERENCE=/root/reference python tests/golden/make_golden.py long
+
+(the second form writes the full-length fixtures listed last below; its N=1024
+run takes over an hour on 8 cores).
 
 Every fixture holds the inputs (or, for N >= 256, a checksum of the seeded
 inputs) and the outputs of the reference's own entry points:
@@ -32,6 +36,9 @@ inputs) and the outputs of the reference's own entry points:
                      spin-boson example and a 6-site chain, and
                      ``HEOMSolver.propagator`` (``_heom_propagator``) on a
                      3-site chain.
+* ``gue256_long.npz``, ``gue1024_long.npz``, ``driven64_long.npz``: the dense
+                     and driven workloads at their full configured lengths
+                     (10000, 1000 and 2000 steps), see ``long_fixtures``.
 """
 from __future__ import annotations
 
@@ -296,11 +303,55 @@ def main():
     api_fixture()
 
 
+def long_fixtures(oqs, which=("driven", "gue256", "gue1024")):
+    """The dense and driven workloads at their full configured lengths.
+
+    * ``gue256_long.npz``  ``_fast_lindblad``, GUE N=256, K=4, 10000 steps:
+                           the final state in full.
+    * ``gue1024_long.npz`` ``_fast_lindblad``, GUE N=1024, K=8, rank-4 rho0,
+                           1000 steps: rows 0..15, the diagonal, the trace and
+                           the Frobenius norm of the final state.
+    * ``driven64_long.npz`` ``LindbladSolver.run`` with ``H = [H0, [mu, f]]``,
+                           2 instances of the driven batch, 2000 steps: the
+                           observable at every step and the final states.
+    Each is written as soon as it is done (the N=1024 run takes over an hour).
+    """
+    if "driven" in which:
+        d = W.driven_batch(n_inst=2, nt=2000)
+        obs_all, rho_all = [], []
+        for b in range(2):
+            E = d["E"]
+
+            def f(t, E=E, dt=d["dt"]):
+                return E[int(round(t / dt)) - 1]
+            Lk = [np.sqrt(d["gamma"][b][k]) * d["L"][b][k] for k in range(2)]
+            sol = oqs.LindbladSolver([csr_matrix(d["H0"][b]), [csr_matrix(d["mu"][b]), f]],
+                                     [csr_matrix(L) for L in Lk])
+            r = sol.run(d["rho0"][b], dt=d["dt"], Nt=d["nt"], e_ops=[csr_matrix(d["O"][b])])
+            obs_all.append(r.observables[:, 0])
+            rho_all.append(r.rholist[-1].toarray())
+        save({"driven64_long": dict(digest=digest(*d["H0"][:2], *d["mu"][:2], *d["rho0"][:2], *d["O"][:2]),
+                                    E=d["E"], dt=d["dt"], nt=d["nt"], observables=np.stack(obs_all),
+                                    rho=np.stack(rho_all))})
+    if "gue256" in which:
+        g = W.gue_instance(N=256, K=4, seed=2)
+        rho = oqs._fast_lindblad(g["H"], g["rho0"].copy(), g["c_ops"], e_ops=[], Nt=g["nt"], dt=g["dt"])
+        save({"gue256_long": dict(digest=digest(g["H"], *g["c_ops"], g["rho0"]), dt=g["dt"], nt=g["nt"],
+                                  rho=rho)})
+    if "gue1024" in which:
+        g = W.gue_instance(N=1024, K=8, scale=0.02, rank=4, seed=4, dt=0.005, nt=1000)
+        rho = oqs._fast_lindblad(g["H"], g["rho0"].copy(), g["c_ops"], e_ops=[], Nt=g["nt"], dt=g["dt"])
+        save({"gue1024_long": dict(digest_ops=digest(g["H"], *g["c_ops"]),
+                                   rho0_diag=np.diag(g["rho0"]).copy(), dt=g["dt"], nt=g["nt"],
+                                   rows=rho[:16, :], diag=np.diag(rho).copy(), trace=np.trace(rho),
+                                   fro=np.linalg.norm(rho))})
+
+
 def save(out):
     for name, arrs in out.items():
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **arrs)
-        print(name, os.path.getsize(path), "bytes")
+        print(name, os.path.getsize(path), "bytes", flush=True)
 
 
 if __name__ == "__main__":
@@ -312,5 +363,7 @@ if __name__ == "__main__":
         save(spectral_fixtures())
     elif sys.argv[1:] == ["api"]:
         api_fixture()
+    elif sys.argv[1:2] == ["long"]:
+        long_fixtures(load(), tuple(sys.argv[2:]) or ("driven", "gue256", "gue1024"))
     else:
         main()

@@ -1,15 +1,15 @@
 """Load the reference's ``pyqed.oqs`` without its package ``__init__``.
 
 Used only by ``make_golden.py`` in a container where the reference sources are
-mounted (read-only) at ``/root/reference``.  ``import pyqed`` fails there
+mounted (read-only); the environment variable ``PYQED_REFERENCE`` names the
+directory that holds the reference's ``pyqed`` package.  ``import pyqed`` fails there
 (missing matplotlib/gbasis and a circular import in ``pyqed/__init__.py:9``
 -> ``pyqed/qchem``), so this registers an empty ``pyqed`` package whose
 ``__path__`` is the reference tree, stubs the plotting packages that
 ``pyqed/signal/sos.py`` and ``pyqed/style.py`` import at module level, then
 imports ``pyqed.phys``, ``pyqed.units``, ``pyqed.mol`` and ``pyqed.oqs``.
 """
-import sys, types, importlib, importlib.abc, importlib.machinery
-REF = '/root/reference'
+import os, sys, types, importlib, importlib.abc, importlib.machinery
 _STUB_ROOTS = ('matplotlib', 'proplot', 'mpl_toolkits')
 
 class _Stub(types.ModuleType):
@@ -34,8 +34,11 @@ class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
 def load():
     if 'pyqed.oqs' in sys.modules:
         return sys.modules['pyqed.oqs']
+    ref = os.environ.get('PYQED_REFERENCE')
+    if not ref or not os.path.isdir(os.path.join(ref, 'pyqed')):
+        raise RuntimeError('set PYQED_REFERENCE to the directory holding the reference pyqed package')
     sys.meta_path.insert(0, _StubFinder())
-    pkg = types.ModuleType('pyqed'); pkg.__path__ = [REF + '/pyqed']
+    pkg = types.ModuleType('pyqed'); pkg.__path__ = [os.path.join(ref, 'pyqed')]
     sys.modules['pyqed'] = pkg
     phys = importlib.import_module('pyqed.phys')
     units = importlib.import_module('pyqed.units')

@@ -36,6 +36,21 @@ def test_candidates():
     assert all("tc_pairs" not in x["options"] for x in c)
 
 
+def test_bf16_candidates_keep_the_fp32_diagonal():
+    # 3xBF16 on instances that fit the tensor-core kernel: only that kernel
+    # (its diagonal of A is applied in FP32), never the GEMM schedule
+    c = autotune.candidates([20, 40, 60, 65], "3xbf16", "diag", 1)
+    assert c == [dict(schedule="auto", options={}), dict(schedule="auto", options={"tc_pairs": 0})]
+    c = autotune.candidates([40, 64], "3xbf16", "none", 0, n_drive=1)
+    assert c == [dict(schedule="auto", options={})]
+    # a driven N = 65 instance, dense collapse operators or N > 65 leave the
+    # tensor-core kernel, and the GEMM schedule is timed again
+    for args in (([65], "diag", 1, 1), ([40], "dense", 2, 0), ([40, 100], "diag", 1, 0)):
+        dims, kind, k, nd = args
+        c = autotune.candidates(dims, "3xbf16", kind, k, n_drive=nd)
+        assert any(x["schedule"] == "gemm" for x in c), args
+
+
 def test_tune_selects_fastest_and_caches(tmp_path, monkeypatch):
     monkeypatch.setenv("PYQED_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
     bi = _batch([20, 40, 60])

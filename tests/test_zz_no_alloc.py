@@ -1,15 +1,19 @@
-"""The no-allocation entry point against the plan-based entry point.
+"""The no-allocation entry point against the plan-based entry point and the
+reference's own results.
 
 ``lgb_propagate_noalloc`` serves callers that cannot allocate device memory
-(a device heap owned by another allocator, or work issued during CUDA-graph
-stream capture): it keeps all working memory in a fixed array inside the
-library.  Here it is called through the C ABI, twice in a row (the second
-call reuses the array the first one left behind), and each result is
-compared with ``lgb_plan_propagate`` in FP64 on the same inputs, within the
-FP64 tolerance of the other parity tests.  This file is named so that pytest
+(a device heap owned by another allocator, or a device-memory budget fixed
+before the library is loaded): it keeps all working memory in a fixed array
+inside the library.  Here it is called through the C ABI, twice in a row
+(the second call reuses the array the first one left behind), and each
+result is compared with ``lgb_plan_propagate`` in FP64 on the same inputs,
+within the FP64 tolerance of the other parity tests; the Jaynes-Cummings
+case is also compared with the reference's own ``LindbladSolver.run``
+output (``tests/golden/jc16.npz``).  This file is named so that pytest
 collects it last.
 """
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -21,6 +25,7 @@ from pyqed_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 @pytest.fixture(scope="module")
@@ -73,6 +78,7 @@ def test_noalloc_matches_plan_entry_point_twice(torch_cuda):
     cases = [
         (jc["H"], jc["c_ops"], C.COPS_DENSE, jc["e_ops"], jc["rho0"], 60, jc["dt"], 1),
         (H64, d64, C.COPS_DIAG, [W.gue_matrix(rng, 64)], np.outer(psi, psi.conj()), 40, 0.01, 0),
+        (H64, [], C.COPS_NONE, [], np.outer(psi, psi.conj()), 25, 0.02, 0),
     ]
     for H, cops, kind, eops, rho0, nt, dt, t0 in cases:
         cops_b = [np.diag(c) for c in cops] if kind == C.COPS_DIAG else cops
@@ -81,7 +87,21 @@ def test_noalloc_matches_plan_entry_point_twice(torch_cuda):
         for _ in range(2):
             obs, rho = _noalloc(torch, H, cops, kind, eops, rho0, nt, dt, t0)
             assert np.abs(rho - ref["rho"][0]).max() < TOL64
-            assert np.abs(obs - ref["observables"][0]).max() < TOL64
+            if eops:
+                assert np.abs(obs - ref["observables"][0]).max() < TOL64
+
+
+def test_noalloc_matches_reference_fixture(torch_cuda):
+    # the reference's LindbladSolver.run on the Jaynes-Cummings system, all
+    # 2000 steps: observables at every step and the states kept in the fixture
+    torch = torch_cuda
+    g = np.load(os.path.join(GOLD, "jc16.npz"))
+    nt = int(g["nt"])
+    for _ in range(2):
+        obs, rho = _noalloc(torch, g["H"], list(g["c_ops"]), C.COPS_DENSE, list(g["e_ops"]),
+                            g["rho0"], nt, float(g["dt"]), 1)
+        assert np.abs(obs - g["observables"]).max() < TOL64
+        assert np.abs(rho - g["states"][-1]).max() < TOL64
 
 
 def test_noalloc_rejects_sizes_beyond_its_limit(torch_cuda):
