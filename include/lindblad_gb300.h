@@ -43,7 +43,9 @@ enum {
   LGB_ERR_TIMEOUT = 5,      /* a bounded device wait gave up                     */
   LGB_ERR_NO_DEVICE = 6,    /* no CUDA device visible                            */
   LGB_ERR_STATE = 7,        /* call order violated (e.g. propagate before set)   */
-  LGB_ERR_TOO_LARGE = 8     /* request exceeds the no-allocation scratch limits  */
+  LGB_ERR_TOO_LARGE = 8,    /* request exceeds the no-allocation scratch limits  */
+  LGB_ERR_CHECK = 9         /* the per-step state check (LGB_OPT_CHECK) exceeded
+                               its tolerance; the propagation itself completed  */
 };
 
 /* ---- precisions ------------------------------------------------------------ */
@@ -136,9 +138,19 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
                        double* obs_out, double* rho_out, double* states_out, void* stream);
 
 /* Copy the per-instance status flags (LGB_OK or LGB_ERR_NONFINITE /
- * LGB_ERR_TIMEOUT) of the last propagate into flags_host[n_inst];
- * synchronises the plan's last stream.  Returns the first non-OK flag. */
+ * LGB_ERR_TIMEOUT / LGB_ERR_CHECK) of the last propagate into
+ * flags_host[n_inst]; synchronises the plan's last stream.  Returns the
+ * first non-OK flag. */
 int lgb_plan_errors(lgb_plan_t plan, int32_t* flags_host);
+
+/* The largest deviations the per-step check (LGB_OPT_CHECK) saw in the last
+ * propagate, per instance: stats_host[2 b] = max over steps of
+ * |Tr rho(t) - Tr rho0|, stats_host[2 b + 1] = max over steps and elements of
+ * |rho_ij - conj(rho_ji)|, or -1 where rho0 itself is not Hermitian (a
+ * correlation seed such as B rho0) and hermiticity is not checked.
+ * Synchronises the plan's last stream.  LGB_ERR_STATE when the check is off.
+ * No counterpart in the reference, which checks neither. */
+int lgb_plan_check_stats(lgb_plan_t plan, double* stats_host);
 
 /* Discrete adjoint of the last lgb_plan_propagate (plans created with
  * LGB_FLAG_ADJOINT: FP32, N <= 64, dense or no collapse operators, no stored
@@ -187,11 +199,24 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
  *                      kernel skip its first MMA commit, so that its bounded
  *                      wait (4096 polls) runs out and every instance it was
  *                      given reports LGB_ERR_TIMEOUT; nothing faults or hangs
+ *   LGB_OPT_CHECK      per-step check of the state, accumulated in FP64:
+ *                      0 (default) off; v = 1..15 checks after every step
+ *                      that |Tr rho(t) - Tr rho0| <= 10^-v and, for
+ *                      instances whose rho0 is Hermitian to 10^-v,
+ *                      max_ij |rho_ij - conj(rho_ji)| <= 10^-v.  An instance
+ *                      that exceeds either is flagged LGB_ERR_CHECK; its
+ *                      propagation completes and its outputs are written
+ *                      (lgb_plan_check_stats gives the deviations).  The
+ *                      state is never renormalised (the RK4 map of a
+ *                      Lindblad generator keeps the trace up to rounding,
+ *                      and trace-zero correlation seeds must stay so).  It
+ *                      is a check, not tuning: it adds one reduction per step.
  * Returns LGB_ERR_INVALID_ARG for an unknown option or value. */
 typedef enum {
   LGB_OPT_TC_PAIRS = 1,
   LGB_OPT_GEMM_WAVES = 2,
-  LGB_OPT_TEST_STALL = 3
+  LGB_OPT_TEST_STALL = 3,
+  LGB_OPT_CHECK = 4
 } lgb_option_t;
 
 int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value);

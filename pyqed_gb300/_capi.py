@@ -24,6 +24,7 @@ LGB_ERR_TIMEOUT = 5
 LGB_ERR_NO_DEVICE = 6
 LGB_ERR_STATE = 7
 LGB_ERR_TOO_LARGE = 8
+LGB_ERR_CHECK = 9
 NOALLOC_MAX_DIM, NOALLOC_MAX_COPS, NOALLOC_MAX_EOPS = 64, 4, 4
 
 # precisions
@@ -38,7 +39,8 @@ SCHED_NAME = {v: k for k, v in SCHED.items()}
 # Every symbol include/lindblad_gb300.h declares.
 EXPORTS = [
     "lgb_get_version", "lgb_status_string", "lgb_plan_create", "lgb_plan_destroy",
-    "lgb_plan_set_operators", "lgb_plan_propagate", "lgb_plan_errors", "lgb_plan_get_info",
+    "lgb_plan_set_operators", "lgb_plan_propagate", "lgb_plan_errors", "lgb_plan_check_stats",
+    "lgb_plan_get_info",
     "lgb_propagate_noalloc", "lgb_plan_adjoint", "lgb_plan_set_option",
     "lgb_redfield_tensor", "lgb_redfield_tensor_batch", "lgb_redfield_max_dim", "lgb_redfield_create", "lgb_redfield_destroy",
     "lgb_redfield_set", "lgb_redfield_propagate", "lgb_redfield_errors",
@@ -47,7 +49,7 @@ EXPORTS = [
     "lgb_spectral_sum", "lgb_spectral_2t",
 ]
 # tuning options (lgb_option_t)
-OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3}
+OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3, "check": 4}
 FLAG_ADJOINT = 1
 HEOM_DOUBLE_FIRST = 1
 HEOM_DIAG_SZ = 2
@@ -132,6 +134,8 @@ def lib():
     L.lgb_plan_propagate.argtypes = [vp, dp, dp, dp, dp, dp, vp]
     L.lgb_plan_errors.restype = ctypes.c_int
     L.lgb_plan_errors.argtypes = [vp, ctypes.POINTER(i32)]
+    L.lgb_plan_check_stats.restype = ctypes.c_int
+    L.lgb_plan_check_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.lgb_plan_get_info.restype = ctypes.c_int
     L.lgb_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
     L.lgb_redfield_tensor.restype = ctypes.c_int

@@ -98,6 +98,7 @@ const char* lgb_status_string(int status) {
     case LGB_ERR_NO_DEVICE: return "no CUDA device";
     case LGB_ERR_STATE: return "call order violated";
     case LGB_ERR_TOO_LARGE: return "size exceeds the no-allocation scratch limit";
+    case LGB_ERR_CHECK: return "per-step trace/hermiticity check exceeded its tolerance";
     default: return "unknown status";
   }
 }
@@ -275,6 +276,8 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
   s = s ? s : dalloc(pl, &pl->d_state, 2 * W * esz);
   s = s ? s : dalloc(pl, &pl->d_y, dense ? (size_t)K * W * esz : 0);
   s = s ? s : dalloc(pl, &pl->d_err, n * sizeof(int));
+  s = s ? s : dalloc(pl, &pl->d_chk, 2 * n * sizeof(double));
+  s = s ? s : dalloc(pl, &pl->d_chkws, sched == LGB_SCHED_GEMM ? 8 * n * sizeof(double) : 0);
   if (s == LGB_OK && pl->d_err) s = cuda_status(cudaMemset(pl->d_err, 0, n * sizeof(int)));
   if (s == LGB_OK && pl->adjoint) {
     const long long W = pl->tot_woff;
@@ -457,6 +460,8 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
   CtaParams p{};
   p.tc_pairs = plan->opt_pairs;
   p.test_stall = plan->opt_stall;
+  p.check_tol = plan->opt_check > 0 ? std::pow(10.0, -plan->opt_check) : 0.0;
+  p.chk = plan->d_chk;
   p.spin = plan->opt_stall ? 4096 : 0;  // the test hook's waits give up after 4096 polls
   p.n_inst = pr.n_inst;
   p.n_cops = pr.n_cops;
@@ -521,6 +526,9 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
       a.obs_out = p.obs_out ? p.obs_out + (long long)b * nrows * pr.n_eops : nullptr;
       a.rho_out = p.rho_out ? p.rho_out + plan->off[b] : nullptr;
       a.states_out = p.states_out ? p.states_out + plan->soff[b] : nullptr;
+      a.check_tol = p.check_tol;
+      a.chk = plan->d_chk + 2 * b;
+      a.chk_ws = plan->d_chkws + 8 * b;
       const int r = lgb::gemm_propagate(a, st);
       if (r != LGB_OK) return r;
     }
@@ -679,9 +687,22 @@ int lgb_plan_errors(lgb_plan_t plan, int32_t* flags_host) {
   return LGB_OK;
 }
 
+int lgb_plan_check_stats(lgb_plan_t plan, double* stats_host) {
+  if (plan == nullptr || stats_host == nullptr) return LGB_ERR_INVALID_ARG;
+  if (plan->opt_check == 0) return LGB_ERR_STATE;
+  cudaError_t e = cudaStreamSynchronize(plan->last_stream);
+  if (e != cudaSuccess) return LGB_ERR_CUDA;
+  e = cudaMemcpy(stats_host, plan->d_chk, 2 * plan->prob.n_inst * sizeof(double), cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
 int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value) {
   if (plan == nullptr) return LGB_ERR_INVALID_ARG;
   switch (option) {
+    case LGB_OPT_CHECK:
+      if (value < 0 || value > 15) return LGB_ERR_INVALID_ARG;
+      plan->opt_check = value;
+      return LGB_OK;
     case LGB_OPT_TC_PAIRS:
       if (value != 0 && value != 1) return LGB_ERR_INVALID_ARG;
       plan->opt_pairs = value;

@@ -89,6 +89,8 @@ struct CtaParams {
   int tc_pairs;              // tensor-core kernel: two instances per CTA for NP <= 32
   int test_stall;            // test hook: the first MMA commit is never issued
   long long spin;            // poll bound of the tensor-core kernel's waits (0: default)
+  double check_tol;          // per-step trace/hermiticity check tolerance (0: off)
+  double* chk;               // [n_inst][2]: max trace drift, max hermiticity deviation (-1: not checked)
 };
 
 }  // namespace lgb

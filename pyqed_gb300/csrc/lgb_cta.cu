@@ -234,8 +234,71 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
     }
   }
 
+  // Optional per-step check (p.check_tol > 0), accumulated in FP64: the drift
+  // |Tr rho(t) - Tr rho0| and, when rho0 is Hermitian to the tolerance,
+  // max_ij |rho_ij - conj(rho_ji)|, both read from the stage-input copy of
+  // the state (X and X^T hold rho after the step).  Thread 0 keeps the
+  // running maxima and writes them, and the LGB_ERR_CHECK flag, at the end.
+  __shared__ double sChk[kMaxWarps][3];
+  const bool checking = p.check_tol > 0.0 && p.chk != nullptr;
+  double2 chk_tr0 = make_double2(0.0, 0.0);
+  bool chk_herm = false, chk_bad = false;
+  double chk_dtr = 0.0, chk_dh = 0.0;
+  auto check_state = [&](bool initial) {
+    double trx = 0.0, try_ = 0.0, hm = 0.0;
+#pragma unroll
+    for (int r = 0; r < ROUNDS; ++r) {
+      if (!act[r]) continue;
+#pragma unroll
+      for (int ii = 0; ii < 4; ++ii) {
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int i = 4 * ty[r] + ii, j = tx[r] + nT * jj;
+          if (i < N && j < N) {
+            const double2 x = to_d2(sX[i * NPS + j]);
+            const double2 xt = to_d2(sXt[i * NPS + j]);  // X^T[i][j] = X[j][i]
+            if (i == j) {
+              trx += x.x;
+              try_ += x.y;
+            }
+            hm = fmax(hm, hypot(x.x - xt.x, x.y + xt.y));
+          }
+        }
+      }
+    }
+    trx = warp_sum(trx);
+    try_ = warp_sum(try_);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) hm = fmax(hm, __shfl_xor_sync(0xffffffffu, hm, o));
+    if (lane == 0) {
+      sChk[warp][0] = trx;
+      sChk[warp][1] = try_;
+      sChk[warp][2] = hm;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double2 tr = make_double2(0.0, 0.0);
+      double h = 0.0;
+      for (int w = 0; w < kWarps; ++w) {
+        tr.x += sChk[w][0];
+        tr.y += sChk[w][1];
+        h = fmax(h, sChk[w][2]);
+      }
+      if (initial) {
+        chk_tr0 = tr;
+        chk_herm = h <= p.check_tol;
+      } else {
+        const double dtr = hypot(tr.x - chk_tr0.x, tr.y - chk_tr0.y);
+        chk_dtr = fmax(chk_dtr, dtr);
+        if (chk_herm) chk_dh = fmax(chk_dh, h);
+        chk_bad = chk_bad || !(dtr <= p.check_tol) || (chk_herm && !(h <= p.check_tol));
+      }
+    }
+  };
+
   if (tid == 0) p.err[b] = 0;
   __syncthreads();
+  if (checking) check_state(true);
   if (p.obs_t0) reduce_state(0);
 
   const int dld = p.drive_ld > 0 ? p.drive_ld : p.nt;
@@ -409,6 +472,7 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
       if (tid == 0) p.err[b] = 4;  // LGB_ERR_NONFINITE
       break;
     }
+    if (checking) check_state(false);
     if (p.store_every > 0 && p.states_out != nullptr && ((step + 1) % p.store_every) == 0) {
       const long long si = (step + 1) / p.store_every - 1;
       double2* dst = p.states_out + p.soff[b] +
@@ -435,6 +499,11 @@ __device__ __forceinline__ void cta_body(const CtaParams& p, const int b, unsign
     }
   }
 
+  if (checking && tid == 0) {
+    p.chk[2 * b] = chk_dtr;
+    p.chk[2 * b + 1] = chk_herm ? chk_dh : -1.0;
+    if (chk_bad && p.err[b] == 0) p.err[b] = 9;  // LGB_ERR_CHECK
+  }
   if (p.rho_out != nullptr) {
     double2* dst = p.rho_out + p.off[b];
 #pragma unroll

@@ -16,6 +16,7 @@
 #include <cublas_v2.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "lgb_internal.h"
 
@@ -321,6 +322,74 @@ __global__ void __launch_bounds__(kEpiThreads) gemm_epilogue_kernel(
 
 __global__ void step_inc_kernel(int* ctr) { *ctr += 1; }
 
+// Per-step check (optional): trace and hermiticity deviation of rho, in FP64.
+// 32 x 32 tiles through shared memory (the transposed tile for rho_ji);
+// the trace partials of the diagonal tiles and the largest |rho_ij -
+// conj(rho_ji)| go to the instance's scratch by atomics (the order of the
+// trace additions only moves its last bits; the check compares with a
+// tolerance).  ws: [0..1] Tr rho0, [2] rho0 Hermitian, [3..4] Tr rho, [5] max
+// deviation (as the bits of a non-negative double).
+template <typename T>
+__global__ void gemm_check_accum_kernel(const void* rho_, int N, double* ws) {
+  using T2 = typename Cplx<T>::type;
+  __shared__ double2 tile[32][33];
+  const T2* rho = reinterpret_cast<const T2*>(rho_);
+  const int ti = blockIdx.y * 32, tj = blockIdx.x * 32;
+  // the transposed tile (rows tj.., columns ti..)
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int i = tj + r, j = ti + threadIdx.x;
+    tile[r][threadIdx.x] = (i < N && j < N) ? to_d2(rho[(long long)i * N + j]) : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  double h = 0.0, tx = 0.0, ty = 0.0;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int i = ti + r, j = tj + threadIdx.x;
+    if (i < N && j < N) {
+      const double2 x = to_d2(rho[(long long)i * N + j]);
+      const double2 xt = tile[threadIdx.x][r];  // rho[j][i]
+      h = fmax(h, hypot(x.x - xt.x, x.y + xt.y));
+      if (i == j) {
+        tx += x.x;
+        ty += x.y;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+    tx += __shfl_xor_sync(0xffffffffu, tx, o);
+    ty += __shfl_xor_sync(0xffffffffu, ty, o);
+  }
+  if (threadIdx.x == 0) {
+    atomicMax(reinterpret_cast<unsigned long long*>(ws + 5), (unsigned long long)__double_as_longlong(h));
+    if (ti == tj) {
+      atomicAdd(ws + 3, tx);
+      atomicAdd(ws + 4, ty);
+    }
+  }
+}
+
+__global__ void gemm_check_fold_kernel(double* ws, double* chk, int* err, double tol, int initial) {
+  const double h = ws[5];
+  if (initial) {
+    ws[0] = ws[3];
+    ws[1] = ws[4];
+    ws[2] = h <= tol ? 1.0 : 0.0;
+    chk[0] = 0.0;
+    chk[1] = ws[2] != 0.0 ? 0.0 : -1.0;
+  } else {
+    const double dtr = hypot(ws[3] - ws[0], ws[4] - ws[1]);
+    chk[0] = fmax(chk[0], dtr);
+    bool bad = !(dtr <= tol);
+    if (ws[2] != 0.0) {
+      chk[1] = fmax(chk[1], h);
+      bad = bad || !(h <= tol);
+    }
+    if (bad && *err == 0) *err = 9;  // LGB_ERR_CHECK
+  }
+  ws[3] = ws[4] = ws[5] = 0.0;
+}
+
 int epi_grid(int N) {
   const long long NN = (long long)N * N;
   long long b = (NN + (long long)kEpiThreads * kEpiElems - 1) / ((long long)kEpiThreads * kEpiElems);
@@ -369,6 +438,8 @@ static int gemm_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
   const size_t esz = sizeof(typename Cplx<T>::type);
   cublasSetStream(a.blas, st);
   gemm_init_kernel<T><<<grid, 256, 0, st>>>(g, a.rho0);
+  const bool check = a.check_tol > 0.0 && a.chk != nullptr;
+  if (check) gemm_check(a, std::is_same<T, double>::value, true, st);
   if (a.obs_t0 && a.E > 0) gemm_obs_kernel<T><<<egrid, kEpiThreads, 0, st>>>(g, a.E, a.obs_out, 0);
   if (cudaMemsetAsync(a.ctr, 0, sizeof(int), st) != cudaSuccess) return LGB_ERR_CUDA;
   if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
@@ -398,6 +469,7 @@ static int gemm_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
         return LGB_ERR_CUDA;
       gemm_epilogue_kernel<T><<<egrid, kEpiThreads, 0, s>>>(g, stage, a.dt, a.diag, a.E, a.obs_out, so);
     }
+    if (check) gemm_check(a, std::is_same<T, double>::value, false, s);
     step_inc_kernel<<<1, 1, 0, s>>>(a.ctr);
     return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
   };
@@ -407,6 +479,17 @@ static int gemm_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
   if (a.nt == 0 && a.rho_out != nullptr)
     cudaMemcpyAsync(a.rho_out, a.rho0, NN * sizeof(double2), cudaMemcpyDeviceToDevice, st);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
+void gemm_check(const GemmRunArgs& a, bool fp64, bool initial, cudaStream_t st) {
+  const int t = (a.g.N + 31) / 32;
+  if (initial) cudaMemsetAsync(a.chk_ws, 0, 8 * sizeof(double), st);
+  if (fp64) {
+    gemm_check_accum_kernel<double><<<dim3(t, t), dim3(32, 8), 0, st>>>(a.g.rho, a.g.N, a.chk_ws);
+  } else {
+    gemm_check_accum_kernel<float><<<dim3(t, t), dim3(32, 8), 0, st>>>(a.g.rho, a.g.N, a.chk_ws);
+  }
+  gemm_check_fold_kernel<<<1, 1, 0, st>>>(a.chk_ws, a.chk, a.g.err, a.check_tol, initial ? 1 : 0);
 }
 
 int gemm_propagate(const GemmRunArgs& a, cudaStream_t st) {

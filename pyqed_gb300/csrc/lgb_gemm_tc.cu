@@ -567,6 +567,8 @@ int split_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
                                                          N, sp.Ls[0], sp.Ls[1], sp.Wp, 0, NP);
   split_trans_kernel<BF16><<<dim3(tiles, tiles), dim3(32, 8), 0, st>>>(
       reinterpret_cast<const float2*>(g.Rbuf), N, N, N, sp.Rs[0], sp.Rs[1], sp.Wp, 0);
+  const bool check = a.check_tol > 0.0 && a.chk != nullptr;
+  if (check) gemm_check(a, false, true, st);
   if (a.obs_t0 && a.E > 0) gemm_obs_split(g, a.E, a.obs_out, st);
   if (cudaMemsetAsync(a.ctr, 0, sizeof(int), st) != cudaSuccess) return LGB_ERR_CUDA;
   if ((e = cudaGetLastError()) != cudaSuccess) return LGB_ERR_CUDA;
@@ -622,6 +624,7 @@ int split_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
       split_epilogue_kernel<BF16><<<tiles * tiles, dim3(32, 8), 0, s>>>(g, sp, stage, a.dt, a.diag, a.E,
                                                                         a.obs_out, so);
     }
+    if (check) gemm_check(a, false, false, s);
     gemm_step_inc(a.ctr, s);
     return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
   };

@@ -160,8 +160,14 @@ struct GemmRunArgs {
   double2* obs_out = nullptr;      // this instance's rows
   double2* rho_out = nullptr;
   double2* states_out = nullptr;
+  double check_tol = 0.0;          // per-step check (0: off)
+  double* chk = nullptr;           // this instance's [2] check maxima
+  double* chk_ws = nullptr;        // this instance's [8] check scratch
 };
 size_t gemm_partial_slots(int N);
+// per-step trace / hermiticity check of the GEMM schedule's state (g.rho,
+// FP32 or FP64): accumulate, then fold into the maxima (initial: the rho0 values)
+void gemm_check(const GemmRunArgs& a, bool fp64, bool initial, cudaStream_t st);
 int gemm_setup(const GemmSetupArgs& a, cudaStream_t st);
 int gemm_propagate(const GemmRunArgs& a, cudaStream_t st);
 // FP32 pieces of the GEMM schedule reused by the split-precision one
@@ -202,6 +208,7 @@ struct lgb_plan {
   int opt_pairs = 1;                       // LGB_OPT_TC_PAIRS
   int opt_waves = 1;                       // LGB_OPT_GEMM_WAVES
   int opt_stall = 0;                       // LGB_OPT_TEST_STALL
+  int opt_check = 0;                       // LGB_OPT_CHECK: 0 off, v: tolerance 10^-v
   cudaStream_t cap_stream = nullptr;       // GEMM schedule: CUDA-graph capture
   int* d_ctr = nullptr;                    // GEMM schedule: device step counter
   void* blas_ws = nullptr;                 // cuBLAS workspace (graph capture allocates nothing)
@@ -239,6 +246,8 @@ struct lgb_plan {
   void* d_state = nullptr;
   void* d_y = nullptr;
   int* d_err = nullptr;
+  double* d_chk = nullptr;                 // [n_inst][2] per-step check maxima
+  double* d_chkws = nullptr;               // [n_inst][8] GEMM schedule: check scratch
   std::vector<void*> allocations;
   // adjoint (plans created with LGB_FLAG_ADJOINT)
   bool adjoint = false;

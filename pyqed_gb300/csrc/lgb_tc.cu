@@ -25,10 +25,19 @@
 // accumulator, and one commit.
 //
 // Each of the 512 threads owns a quarter of the columns of one TMEM lane (one
-// component of one row); it keeps rho, the RK4 sum, a Kahan compensation term
-// and the stage input in registers, performs the RK4 stage combination
-// (pyqed/phys.py:1051-1064) with a Kahan-compensated final update, splits the
-// next stage input into hi/lo and writes it into the XM and X^T buffers.
+// component of one row); it keeps rho and a Kahan compensation term in
+// registers, forms the next stage input of the RK4 step in Horner form (below)
+// with a Kahan-compensated final update, splits it into hi/lo and writes it
+// into the XM and X^T buffers.
+//
+// RK4 (pyqed/phys.py:1051-1064) in Horner form.  Within a step the generator
+// L is fixed (a static H, or H(t_{k+1}) frozen for the step, as
+// pyqed/oqs.py:1790-1796), so the classic map rho -> rho + h/6 (k1 + 2 k2 +
+// 2 k3 + k4) is exactly the degree-4 Taylor polynomial of hL applied to rho,
+// evaluated here as
+//   y1 = rho + h/4 L rho,  y2 = rho + h/3 L y1,  y3 = rho + h/2 L y2,
+//   rho' = rho + h L y3,
+// the same map with no RK4 sum to carry between stages.
 // With BF16 operands the diagonal of A stays out of the split products: its
 // entries are of order one (the site energies) and BF16 hi + lo holds them
 // only to ~2^-17 relative, which turns into a phase error growing with t.
@@ -91,6 +100,7 @@ struct TcShared {
   uint32_t tmem_base;
   int next[2];
   float2 red[2][kMaxEops][kWarps];  // per-warp observable partials
+  double chk[2][kWarps][3];         // per-warp check partials: Tr rho (re, im), max hermiticity deviation
 };
 
 // N = 65 (static H): the 64 x 64 block runs on the tensor cores as above; the
@@ -108,7 +118,7 @@ struct TcShared {
 constexpr int kBorder = 65;  // border index 64 plus one (the corner is entry 64 of the row arrays)
 struct TcBorder {
   float2 bx[2][2][kBorder];   // stage input [buffer][0: column c_i, 1: row r_j and corner]
-  float2 rho[2][kBorder], racc[2][kBorder], nkc[2][kBorder];
+  float2 rho[2][kBorder], nkc[2][kBorder];
   float2 aB[kBorder], bB[kBorder];      // A[i][g], A[g][j] (entry 64: alpha)
   float2 dcol[kBorder], drow[kBorder];  // D[i][g], D[g][j]
   float2 t1[64], t3[64], t4[64];        // (A_M c)_i, (b^T M)_j, (conj(A_M) r)_j of the stage
@@ -309,7 +319,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const long long wo = p.woff[b];
   const int E = p.n_eops;
   const bool diag = p.cops_kind == 2 && p.n_cops > 0;
-  const float half_dt = (float)(0.5 * p.dt), dt = (float)p.dt, sixth_dt = (float)(p.dt / 6.0);
+  const float dt = (float)p.dt;
 
   unsigned char* SA = smem + G::OFF_A;
   unsigned char* SXM = smem + G::OFF_XM;
@@ -368,33 +378,65 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   // (8-byte stores of the 32 rows of a warp, 1 KB apart per row group, would
   // share one bank set).  Every caller walks the groups in order.
   constexpr bool kXmPairs = BF16 && (NPQ % 8 == 0);
-  [[maybe_unused]] float xmh[4], xml[4];
+  [[maybe_unused]] uint32_t xph[2], xpl[2];  // BF16: packed XM values of the even group
+  // XM row sign as a bit mask on packed BF16 pairs (c = 0: the row holds -Xr)
+  [[maybe_unused]] const uint32_t xm_flip = c == 0 ? 0x80008000u : 0u;
   auto write_group = [&](int g, const float* x4) {
     if (!row_ok) return;
-    float vh[4], vl[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) El::split(x4[e], vh[e], vl[e]);  // split(-x) = -split(x)
     const int col = j0 + g * 4;
+    if constexpr (BF16) {
+      // split on packed pairs: hi = bf16(x) (two at a time), lo = bf16(x - hi);
+      // the same values as Elem<true>::split, with fewer conversions
+      uint32_t h[2], l[2];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const uint32_t o = off_t<BF16, NP>(ncol(c, col + e), i);
-      *reinterpret_cast<ET*>(SXT + o) = (ET)vh[e];
-      *reinterpret_cast<ET*>(SXT + G::LVL_T + o) = (ET)vl[e];
-      vh[e] *= xm_sign;
-      vl[e] *= xm_sign;
-    }
-    if constexpr (kXmPairs) {
-      if ((g & 1) == 0) {
+      for (int q = 0; q < 2; ++q) {
+        const __nv_bfloat162 hb = __floats2bfloat162_rn(x4[2 * q], x4[2 * q + 1]);
+        const float2 hf = __bfloat1622float2(hb);
+        const float2 r = __fadd2_rn(make_float2(x4[2 * q], x4[2 * q + 1]), make_float2(-hf.x, -hf.y));
+        const __nv_bfloat162 lb = __floats2bfloat162_rn(r.x, r.y);
+        h[q] = *reinterpret_cast<const uint32_t*>(&hb);
+        l[q] = *reinterpret_cast<const uint32_t*>(&lb);
+      }
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          xmh[e] = vh[e];
-          xml[e] = vl[e];
+      for (int e = 0; e < 4; ++e) {
+        const uint32_t o = off_t<BF16, NP>(ncol(c, col + e), i);
+        const int sh16 = (e & 1) * 16;
+        *reinterpret_cast<uint16_t*>(SXT + o) = (uint16_t)(h[e >> 1] >> sh16);
+        *reinterpret_cast<uint16_t*>(SXT + G::LVL_T + o) = (uint16_t)(l[e >> 1] >> sh16);
+      }
+      // -bf16(x) = bf16(-x) exactly: the XM sign is a flip of the sign bits
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        h[q] ^= xm_flip;
+        l[q] ^= xm_flip;
+      }
+      if constexpr (kXmPairs) {
+        if ((g & 1) == 0) {
+          xph[0] = h[0];
+          xph[1] = h[1];
+          xpl[0] = l[0];
+          xpl[1] = l[1];
+        } else {
+          *reinterpret_cast<uint4*>(SXM + off_s<BF16, NP>(xm_row, col - 4)) = make_uint4(xph[0], xph[1], h[0], h[1]);
+          *reinterpret_cast<uint4*>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col - 4)) =
+              make_uint4(xpl[0], xpl[1], l[0], l[1]);
         }
       } else {
-        st8_bf16(SXM + off_s<BF16, NP>(xm_row, col - 4), xmh, vh);
-        st8_bf16(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col - 4), xml, vl);
+        *reinterpret_cast<uint2*>(SXM + off_s<BF16, NP>(xm_row, col)) = make_uint2(h[0], h[1]);
+        *reinterpret_cast<uint2*>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col)) = make_uint2(l[0], l[1]);
       }
     } else {
+      float vh[4], vl[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) El::split(x4[e], vh[e], vl[e]);  // split(-x) = -split(x)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const uint32_t o = off_t<BF16, NP>(ncol(c, col + e), i);
+        *reinterpret_cast<ET*>(SXT + o) = (ET)vh[e];
+        *reinterpret_cast<ET*>(SXT + G::LVL_T + o) = (ET)vl[e];
+        vh[e] *= xm_sign;
+        vl[e] *= xm_sign;
+      }
       st4<BF16>(SXM + off_s<BF16, NP>(xm_row, col), vh);
       st4<BF16>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col), vl);
     }
@@ -447,7 +489,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   // ---- state: element jj of this thread is component .x (jj even) or .y (jj
   // odd) of pair jj / 2, so the RK4 arithmetic runs on packed FP32x2 pairs;
   // nkc holds the negated Kahan compensation.
-  float2 rho2[NPQ / 2], racc2[NPQ / 2], nkc2[NPQ / 2];
+  float2 rho2[NPQ / 2], nkc2[NPQ / 2];
   auto rho_at = [&](int jj) -> float { return (jj & 1) ? rho2[jj >> 1].y : rho2[jj >> 1].x; };
 
   // ---- observables Tr[O rho]: FP32 partials per thread and warp (pairwise
@@ -468,7 +510,85 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   }
   // Part 1 (no barrier): per-warp partials of every Tr[O_e rho] into sh.red;
   // returns whether this thread's elements are finite.
+  // ---- optional per-step check (p.check_tol > 0), FP64 accumulation: the
+  // drift |Tr rho(t) - Tr rho0| and, for a Hermitian rho0, max_ij
+  // |rho_ij - conj(rho_ji)|.  Both sides of the hermiticity test are read
+  // from the X^T operand buffer (hi + lo, the stage input = rho after the
+  // step), so that an exactly Hermitian FP32 state compares equal; the
+  // resolution is that of the split operands.  Thread 0 of the group keeps
+  // the running maxima.
+  const bool checking = p.check_tol > 0.0 && p.chk != nullptr;
+  double2 chk_tr0 = make_double2(0.0, 0.0);
+  bool chk_herm = false, chk_bad = false;
+  double chk_dtr = 0.0, chk_dh = 0.0;
+  auto xt_at = [&](int r, int k) -> float {  // component of X^T row r, K index k (hi + lo)
+    const uint32_t o = off_t<BF16, NP>(r, k);
+    return (float)*reinterpret_cast<const ET*>(SXT + o) + (float)*reinterpret_cast<const ET*>(SXT + G::LVL_T + o);
+  };
+  auto check_partials = [&]() {
+    float tr = 0.f, hf = 0.f;
+    if (i < N) {
+#pragma unroll 1
+      for (int jj = 0; jj < NPQ; ++jj) {
+        const int j = j0 + jj;
+        if (j < N) {
+          const float a = xt_at(ncol(c, j), i), t = xt_at(ncol(c, i), j);  // rho_ij, rho_ji (component c)
+          if (j == i) tr = a;
+          hf = fmaxf(hf, fabsf(c == 0 ? a - t : a + t));  // exact for the split values of a Hermitian state
+        }
+      }
+    }
+    // both components of each element: the partner lane holds the other one
+    const double hp = (double)__shfl_xor_sync(0xffffffffu, hf, 16);
+    double hm = sqrt((double)hf * (double)hf + hp * hp);
+    double trx = c == 0 ? (double)tr : 0.0, tri = c == 1 ? (double)tr : 0.0;
+    if constexpr (BD) {
+      if (tid < kG) {  // border column (t, g) against row (g, t); the corner in the trace
+        const float2 a = bd->rho[0][tid], t = bd->rho[1][tid];
+        const double dx = (double)a.x - (double)t.x, dy = (double)a.y + (double)t.y;
+        hm = fmax(hm, sqrt(dx * dx + dy * dy));
+      } else if (tid == kG) {
+        const float2 z = bd->rho[1][kG];
+        trx += (double)z.x;
+        tri += (double)z.y;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      trx += __shfl_xor_sync(0xffffffffu, trx, o);
+      tri += __shfl_xor_sync(0xffffffffu, tri, o);
+      hm = fmax(hm, __shfl_xor_sync(0xffffffffu, hm, o));
+    }
+    if (lane == 0) {
+      sh.chk[grp][warp][0] = trx;
+      sh.chk[grp][warp][1] = tri;
+      sh.chk[grp][warp][2] = hm;
+    }
+  };
+  // after a barrier that follows check_partials
+  auto check_fold = [&](bool initial) {
+    if (tid != 0) return;
+    double2 tr = make_double2(0.0, 0.0);
+    double h = 0.0;
+    for (int w = 0; w < kW; ++w) {
+      tr.x += sh.chk[grp][w][0];
+      tr.y += sh.chk[grp][w][1];
+      h = fmax(h, sh.chk[grp][w][2]);
+    }
+    if (initial) {
+      chk_tr0 = tr;
+      chk_herm = h <= p.check_tol;
+    } else {
+      const double ex = tr.x - chk_tr0.x, ey = tr.y - chk_tr0.y;
+      const double dtr = sqrt(ex * ex + ey * ey);
+      chk_dtr = fmax(chk_dtr, dtr);
+      if (chk_herm) chk_dh = fmax(chk_dh, h);
+      chk_bad = chk_bad || !(dtr <= p.check_tol) || (chk_herm && !(h <= p.check_tol));
+    }
+  };
+
   auto obs_partials = [&]() -> bool {
+    if (checking) check_partials();
     bool fin = true;
     if (i < N) {
 #pragma unroll
@@ -527,6 +647,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   // element was not finite.
   auto obs_finish = [&](bool fin, int row) -> bool {
     const bool anybad = gor<GR>(grp, !fin);
+    if (checking) check_fold(false);
     if (p.obs_out != nullptr) {
       for (int e = warp; e < E; e += kW) {
         float2 v = lane < kW ? sh.red[grp][e][lane] : make_float2(0.f, 0.f);
@@ -573,7 +694,6 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         rho2[jj >> 1].y = (float)v;
       } else {
         rho2[jj >> 1].x = (float)v;
-        racc2[jj >> 1] = make_float2(0.f, 0.f);
         nkc2[jj >> 1] = make_float2(0.f, 0.f);
       }
     }
@@ -625,7 +745,6 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       const float2 v = make_float2((float)z.x, (float)z.y);
       bd->rho[sl][t] = v;
       bd->bx[0][sl][t] = v;
-      bd->racc[sl][t] = make_float2(0.f, 0.f);
       bd->nkc[sl][t] = make_float2(0.f, 0.f);
     }
     gsync<GR>(grp);
@@ -750,18 +869,13 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         }
         const float2 rh = bd->rho[sl][t];
         float2 xn;
-        if (stage == 0) {
-          bd->racc[sl][t] = R;
-          xn = make_float2(fmaf(half_dt, R.x, rh.x), fmaf(half_dt, R.y, rh.y));
-        } else if (stage < 3) {
-          const float2 ra = bd->racc[sl][t];
-          bd->racc[sl][t] = make_float2(fmaf(2.f, R.x, ra.x), fmaf(2.f, R.y, ra.y));
-          const float h = stage == 2 ? dt : half_dt;
+        if (stage < 3) {
+          const float h = (float)(p.dt / (4 - stage));  // the block's Horner coefficient
           xn = make_float2(fmaf(h, R.x, rh.x), fmaf(h, R.y, rh.y));
         } else {
-          // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4), as the block
-          const float2 ra = bd->racc[sl][t], nk = bd->nkc[sl][t];
-          const float yx = fmaf(sixth_dt, ra.x + R.x, nk.x), yy = fmaf(sixth_dt, ra.y + R.y, nk.y);
+          // Kahan-compensated rho += h L y3, as the block
+          const float2 nk = bd->nkc[sl][t];
+          const float yx = fmaf(dt, R.x, nk.x), yy = fmaf(dt, R.y, nk.y);
           const float tx = rh.x + yx, ty = rh.y + yy;
           bd->nkc[sl][t] = make_float2(yx - (tx - rh.x), yy - (ty - rh.y));
           xn = make_float2(tx, ty);
@@ -772,6 +886,12 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     }
   };
   if (tid == 0) p.err[b] = 0;
+  if (checking) {  // the values of rho0 (the X^T buffer written above)
+    gsync<GR>(grp);
+    check_partials();
+    gsync<GR>(grp);
+    check_fold(true);
+  }
   if (p.obs_t0) obs_finish(obs_partials(), 0);
   // The observables of step s are reduced while the MMAs of the first stage
   // of step s + 1 run (and after the loop for the last step).
@@ -825,15 +945,17 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       }
       fence_after_sync();
       // RHS element R = (combined accumulator) + (D o X); stages 0-2 form the
-      // RK4 sum and the next stage input, stage 3 applies the Kahan-compensated
+      // next Horner stage input, stage 3 applies the Kahan-compensated
       // update.  Each group of 4 columns (never crossing a 16-block) is loaded
       // from TMEM, combined with the partner lane, updated and written straight
       // into the operand buffers of the next stage.
-      const float2 cst2 = make_float2(stage == 2 ? dt : half_dt, stage == 2 ? dt : half_dt);
+      // Horner coefficient of the stage: y_{s+1} = rho + h/(4 - s) L y_s
+      const float cstf = stage == 3 ? dt : (float)(p.dt / (4 - stage));
+      const float2 cst2 = make_float2(cstf, cstf);
       // MODE 0: no diagonal dissipator term in this warp, 1: pure dephasing
       // (diagonal real D) in a warp that holds diagonal elements, 2: general
-      // diagonal D.  STAGE 0, 1 (stages 1 and 2) or 3.  Mode and stage are
-      // resolved outside the unrolled element loops.
+      // diagonal D.  STAGE 0 (stages 0-2) or 3.  Mode and stage are resolved
+      // outside the unrolled element loops.
       auto epilogue = [&](auto mode_tag, auto stage_tag) {
         constexpr int MODE = decltype(mode_tag)::value;
         constexpr int STAGE = decltype(stage_tag)::value;
@@ -894,15 +1016,11 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
               R.x = fmaf(u0, r0.x, fmaf(u1, r0.y, fmaf(u2, a0.x, fmaf(u3, a0.y, R.x))));
               R.y = fmaf(u0, r1.x, fmaf(u1, r1.y, fmaf(u2, a1.x, fmaf(u3, a1.y, R.y))));
             }
-            if constexpr (STAGE == 0) {
-              racc2[k] = R;
-              xn2[h] = __ffma2_rn(cst2, R, rho2[k]);
-            } else if constexpr (STAGE == 1) {
-              racc2[k] = __ffma2_rn(make_float2(2.f, 2.f), R, racc2[k]);
+            if constexpr (STAGE < 3) {
               xn2[h] = __ffma2_rn(cst2, R, rho2[k]);
             } else {
-              // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4)
-              const float2 y = __ffma2_rn(make_float2(sixth_dt, sixth_dt), __fadd2_rn(racc2[k], R), nkc2[k]);
+              // Kahan-compensated rho += h L y3
+              const float2 y = __ffma2_rn(cst2, R, nkc2[k]);
               const float2 t = __fadd2_rn(rho2[k], y);
               nkc2[k] = __ffma2_rn(__ffma2_rn(rho2[k], m1, t), m1, y);  // y - (t - rho)
               rho2[k] = t;
@@ -935,7 +1053,6 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         }
       };
       using S0 = std::integral_constant<int, 0>;
-      using S1 = std::integral_constant<int, 1>;
       using S3 = std::integral_constant<int, 3>;
       const int mode = !diag ? 0 : (dfast ? (dwarp ? 1 : 0) : 2);
       auto by_mode = [&](auto stage_tag) {
@@ -943,8 +1060,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         else if (mode == 1) epilogue(std::integral_constant<int, 1>{}, stage_tag);
         else epilogue(std::integral_constant<int, 2>{}, stage_tag);
       };
-      if (stage == 0) by_mode(S0{});
-      else if (stage < 3) by_mode(S1{});
+      if (stage < 3) by_mode(S0{});
       else by_mode(S3{});
       bcur ^= 1;
     }
@@ -970,8 +1086,16 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
     }
   }
 
-  if (alive && !nonfinite && pend_row >= 0) nonfinite = obs_finish(obs_partials(), pend_row);
+  if (alive && !nonfinite && pend_row >= 0) {
+    if (checking) gsync<GR>(grp);  // the last epilogue's X^T writes
+    nonfinite = obs_finish(obs_partials(), pend_row);
+  }
   if (nonfinite && tid == 0) p.err[b] = 4;  // LGB_ERR_NONFINITE
+  if (checking && tid == 0) {
+    p.chk[2 * b] = chk_dtr;
+    p.chk[2 * b + 1] = chk_herm ? chk_dh : -1.0;
+    if (chk_bad && p.err[b] == 0) p.err[b] = 9;  // LGB_ERR_CHECK
+  }
   if (alive && p.rho_out != nullptr && i < N) {
     double2* dst = p.rho_out + p.off[b];
 #pragma unroll

@@ -117,9 +117,30 @@ class Propagator:
 
     def set_option(self, name, value):
         """Option of the plan (``lgb_plan_set_option``): ``tc_pairs`` (0/1),
-        ``gemm_waves`` (1/2), or the error-path test hook ``test_stall`` (0/1)."""
+        ``gemm_waves`` (1/2), ``check`` (0 off, v: the per-step trace and
+        hermiticity check at tolerance 10^-v), or the error-path test hook
+        ``test_stall`` (0/1)."""
         C.check(self._lib.lgb_plan_set_option(self._plan, C.OPT[name], int(value)),
                 "lgb_plan_set_option")
+
+    def set_check(self, tol):
+        """Per-step FP64 check of trace and hermiticity at tolerance ``tol``
+        (rounded to a power of ten, 1e-1 .. 1e-15); None or 0 turns it off."""
+        if not tol:
+            self.set_option("check", 0)
+            return
+        v = int(round(-np.log10(float(tol))))
+        if not 1 <= v <= 15:
+            raise ValueError("check tolerance must lie in [1e-15, 1e-1]")
+        self.set_option("check", v)
+
+    def check_stats(self):
+        """(n_inst, 2) array of the last propagate's largest |Tr rho(t) -
+        Tr rho0| and max_ij |rho_ij - conj(rho_ji)| (-1: rho0 not Hermitian,
+        hermiticity not checked)."""
+        buf = (ctypes.c_double * (2 * self.n_inst))()
+        C.check(self._lib.lgb_plan_check_stats(self._plan, buf), "lgb_plan_check_stats")
+        return np.array(buf[:], dtype=np.float64).reshape(self.n_inst, 2)
 
     def info(self):
         inf = C.PlanInfo()
@@ -180,10 +201,20 @@ class Propagator:
         return np.array(flags[:], dtype=np.int32)
 
     def check_errors(self):
+        """Raise on the first failed instance; instances that only failed the
+        per-step check (their outputs are complete) give a RuntimeWarning.
+        Returns the per-instance flags."""
         f = self.errors()
-        bad = np.nonzero(f)[0]
+        bad = np.nonzero((f != C.LGB_OK) & (f != C.LGB_ERR_CHECK))[0]
         if bad.size:
             raise C.LindbladError(int(f[bad[0]]), "instance %d" % int(bad[0]))
+        flagged = np.nonzero(f == C.LGB_ERR_CHECK)[0]
+        if flagged.size:
+            import warnings
+            warnings.warn("%d instance(s) exceeded the per-step trace/hermiticity check "
+                          "tolerance (first: %d)" % (flagged.size, int(flagged[0])), RuntimeWarning,
+                          stacklevel=2)
+        return f
 
     # -- unpacking -------------------------------------------------------------------
     def unpack_obs(self, obs):

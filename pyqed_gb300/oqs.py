@@ -15,7 +15,8 @@ correlation entry points, the same ``Result`` fields and row conventions:
 
 Extensions are keyword-only: ``precision`` ('fp64' default = the
 reference's complex128; 'fp32', '3xtf32', '3xbf16'), ``schedule``,
-``store_states``, ``rholist_format`` and ``device``.  Inputs may be numpy,
+``store_states``, ``rholist_format``, ``nout`` (keep every nout-th step),
+``check`` (per-step FP64 trace/hermiticity check) and ``device``.  Inputs may be numpy,
 scipy.sparse or torch (the reference's ``run`` accepts only scipy.sparse).
 Collapse operators that are all diagonal are passed to the kernels as
 diagonals (an exact rewrite of the same RHS).
@@ -116,7 +117,7 @@ class LindbladSolver:
 
     # -- core --------------------------------------------------------------------
     def _propagate(self, rho0, dt, Nt, e_ops, *, t0=0.0, obs_t0=True, store_states=False,
-                   precision=None, H=None):
+                   precision=None, H=None, store_every=1, check=None):
         H = self.H if H is None else H
         if isinstance(H, list):
             H0 = to_dense(H[0])
@@ -130,10 +131,14 @@ class LindbladSolver:
         e_list = [to_dense(e) for e in (e_ops or [])]
         kind, K, cops = _cops_for_engine(self.c_ops)
         prop = Propagator([N], nt=Nt, dt=dt, n_cops=K, cops_kind=kind, n_eops=len(e_list),
-                          n_drive=len(terms), obs_t0=obs_t0, store_every=1 if store_states else 0,
+                          n_drive=len(terms), obs_t0=obs_t0,
+                          store_every=store_every if store_states else 0,
                           precision=precision or self.precision, schedule=self.schedule,
                           drive_shared=True, device=self.device)
+        self.last_check = None
         try:
+            if check:
+                prop.set_check(check)
             prop.set_operators(H0, cops, pack(e_list) if e_list else None,
                                pack([h for h, _ in terms]) if terms else None)
             drive = None
@@ -142,7 +147,12 @@ class LindbladSolver:
                 drive = torch.from_numpy(_eval_drive(terms, Nt, dt, t0).ravel()).to(prop.device)
             out = prop.alloc_outputs(want_obs=True, want_rho=True, want_states=store_states)
             obs, rho, st = prop.propagate_device(prop.to_device(rho0), drive, out)
-            prop.check_errors()
+            flags = prop.check_errors()
+            if check:
+                tr, he = prop.check_stats()[0]
+                self.last_check = dict(tolerance=float(check), trace_drift=float(tr),
+                                       hermiticity=None if he < 0 else float(he),
+                                       ok=bool(flags[0] == 0))
             nrows = Nt + int(obs_t0)
             obs_h = prop.unpack_obs(obs)[0] if obs is not None else np.zeros((nrows, 0), complex)
             rho_h = prop.unpack_rho(rho)[0]
@@ -160,12 +170,27 @@ class LindbladSolver:
         return [s.copy() for s in states]
 
     def run(self, rho0, dt, Nt, t0=0., e_ops=None, return_result=True, *, precision=None,
-            store_states=True, rholist_format="csr"):
-        """Propagate Nt RK4 steps (``pyqed/oqs.py:1149-1187``)."""
+            store_states=True, rholist_format="csr", nout=1, check=None):
+        """Propagate Nt RK4 steps (``pyqed/oqs.py:1149-1187``).
+
+        ``nout`` (keyword extension; the reference's ``Result`` carries it,
+        ``pyqed/mol.py:98-114``): keep every nout-th step only.  The states
+        after steps nout, 2 nout, ... go to ``rholist`` and the observables of
+        those steps (plus t0 on the static path) to ``observables``, so that
+        the rows match ``Result.times`` = t0 + arange(Nt // nout + 1) dt nout.
+
+        ``check=tol`` (keyword extension) checks after every step, in FP64 on
+        the GPU, that the trace and (for a Hermitian rho0) the hermiticity of
+        rho stay within ``tol``; the result's ``check`` attribute holds the
+        largest deviations.  The state is not renormalised.
+        """
+        nout = int(nout)
+        if nout < 1:
+            raise ValueError("nout must be >= 1")
         if isinstance(self.H, list):
             obs, rho, st = self._propagate(rho0, dt, Nt, e_ops, t0=t0, obs_t0=False,
                                            store_states=store_states and return_result,
-                                           precision=precision)
+                                           precision=precision, store_every=nout, check=check)
             if not return_result:
                 # pyqed/oqs.py:1745-1780: observables to obs.dat, den_mat.dat
                 # opened (and left empty), the final state returned
@@ -177,28 +202,33 @@ class LindbladSolver:
                         f.write(fmt.format(t, *obs[k]))
                 open("den_mat.dat", "w").close()
                 return csr_matrix(rho) if rholist_format == "csr" else rho
-            result = Result(dt=dt, Nt=Nt, rho0=rho0)
-            result.observables = obs
+            result = Result(dt=dt, Nt=Nt, rho0=rho0, nout=nout)
+            result.observables = obs[nout - 1::nout] if nout > 1 else obs
             result.rholist = self._as_list(st, rholist_format)
+            if check:
+                result.check = self.last_check
             return result
         obs, rho, st = self._propagate(rho0, dt, Nt, e_ops, obs_t0=True,
-                                       store_states=store_states, precision=precision)
-        result = Result(dt=dt, Nt=Nt, rho0=rho0)
-        result.observables = obs
+                                       store_states=store_states, precision=precision,
+                                       store_every=nout, check=check)
+        result = Result(dt=dt, Nt=Nt, rho0=rho0, nout=nout)
+        result.observables = obs[::nout] if nout > 1 else obs
         result.rholist = self._as_list(st, rholist_format)
+        if check:
+            result.check = self.last_check
         return result
 
     evolve = run
 
     def evolve_fast(self, rho0, dt, Nt, t0=0., e_ops=None, return_result=True, fast=True, *,
-                    precision=None):
+                    precision=None, check=None):
         """Final state after Nt steps (``_fast_lindblad``, ``pyqed/oqs.py:1492-1594``).
 
         Like the reference, a writable complex ndarray ``rho0`` is overwritten
         with the final state.  Unlike it, ``e_ops=None`` is accepted.
         """
         _, rho, _ = self._propagate(rho0, dt, Nt, None, obs_t0=False, store_states=False,
-                                    precision=precision)
+                                    precision=precision, check=check)
         if isinstance(rho0, np.ndarray) and np.iscomplexobj(rho0) and rho0.flags.writeable:
             rho0[...] = rho
             return rho0

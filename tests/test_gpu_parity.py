@@ -84,6 +84,33 @@ def test_driven_run_golden(golden, prec, tol):
         assert np.abs(r.rholist[-1].toarray() - g["rho"][b]).max() < tol
 
 
+def test_run_nout_keeps_every_nth_step(golden):
+    # the reference's Result.times for nout (pyqed/mol.py:113); rows and states
+    # are those of the full run at the kept steps
+    g = golden("jc16")
+    sol = LindbladSolver(csr_matrix(g["H"]), [csr_matrix(c) for c in g["c_ops"]])
+    e_ops = [csr_matrix(e) for e in g["e_ops"]]
+    r = sol.run(g["rho0"], dt=float(g["dt"]), Nt=int(g["nt"]), e_ops=e_ops, nout=5)
+    assert r.times.shape == (int(g["nt"]) // 5 + 1,) and r.nout == 5
+    assert r.observables.shape == r.times.shape + (2,)
+    assert np.abs(r.observables - g["observables"][::5]).max() < TOL64
+    assert len(r.rholist) == int(g["nt"]) // 5
+    for k, st in zip(g["state_index"], g["states"]):
+        if (k + 1) % 5 == 0:
+            assert np.abs(r.rholist[(k + 1) // 5 - 1].toarray() - st).max() < TOL64
+    d = golden("driven64")
+    dt, nt = float(d["dt"]), int(d["nt"])
+    E = d["E"]
+    sol = LindbladSolver([csr_matrix(d["H0"][0]), [csr_matrix(d["mu"][0]),
+                          lambda t, E=E: E[int(round(t / dt)) - 1]]],
+                         [csr_matrix(L) for L in d["L"][0]])
+    r = sol.run(d["rho0"][0], dt=dt, Nt=nt, e_ops=[csr_matrix(d["O"][0])], nout=3)
+    assert r.observables.shape == (nt // 3, 1)
+    assert np.abs(r.observables[:, 0] - d["observables"][0][2::3]).max() < TOL64
+    assert len(r.rholist) == nt // 3
+    assert np.abs(r.rholist[-1].toarray() - d["rho"][0]).max() < TOL64  # 30 = 10 x 3
+
+
 def test_correlation_entry_points_golden(golden, tmp_path):
     g = golden("corr_jc")
     jc = W.jaynes_cummings()
