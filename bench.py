@@ -42,12 +42,17 @@ UNIT = "instance-steps/s"
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
-def make_workload(name, n_inst=None, nt=None):
+def make_workload(name, n_inst=None, nt=None, shard=None):
+    """The bench workloads.  ``shard=(rank, world)`` keeps this rank's share of
+    the instances (``pyqed_gb300.shard.partition``: greedy balance of N^3);
+    ``desc`` still describes the whole job."""
     from pyqed_gb300 import workloads as W
     from pyqed_gb300.batch import prepare_batch
+    from pyqed_gb300.shard import shard_indices
     if name == "exciton4096":
         n_inst = n_inst or 4096
-        ex = W.exciton_batch(n_inst=n_inst)
+        idx = None if shard is None else shard_indices(W.exciton_dims(n_inst=n_inst), *shard)
+        ex = W.exciton_batch(n_inst=n_inst, indices=idx)
         nt = nt or ex["nt"]
         cops = [[np.diag(c) for c in cd] for cd in ex["c_diag"]]
         seeds = [m @ r for m, r in zip(ex["mu"], ex["rho_g"])]
@@ -58,26 +63,29 @@ def make_workload(name, n_inst=None, nt=None):
                     output="C(t)=Tr[mu rho(t)], (n_inst, nt) complex")
         flops = int(64 * np.sum(bi.dims.astype(np.int64) ** 3))
         return dict(bi=bi, nt=nt, dt=ex["dt"], obs_t0=False, drive=None, desc=desc,
-                    flops_per_step=flops, ex=ex)
+                    flops_per_step=flops, ex=ex, n_total=n_inst)
     if name == "driven256":
         n_inst = n_inst or 256
         d = W.driven_batch(n_inst=n_inst, nt=nt or 2000)
         nt = d["nt"]
-        cops = [[np.sqrt(d["gamma"][b][k]) * d["L"][b][k] for k in range(2)] for b in range(n_inst)]
-        bi = prepare_batch(d["H0"], cops, d["rho0"], [[o] for o in d["O"]],
-                           drive_ops=[[m] for m in d["mu"]])
+        sel = list(range(n_inst)) if shard is None else [int(b) for b in shard_indices(np.full(n_inst, 64), *shard)]
+        cops = [[np.sqrt(d["gamma"][b][k]) * d["L"][b][k] for k in range(2)] for b in sel]
+        bi = prepare_batch([d["H0"][b] for b in sel], cops, [d["rho0"][b] for b in sel],
+                           [[d["O"][b]] for b in sel], drive_ops=[[d["mu"][b]] for b in sel])
         desc = dict(workload=name, n_inst=n_inst, nt=nt, dt=d["dt"], N=64, K=2,
                     drive="H(t)=H0-E(t)mu, shared GP pulse")
         flops = int(64 * 3 * np.sum(bi.dims.astype(np.int64) ** 3))
         return dict(bi=bi, nt=nt, dt=d["dt"], obs_t0=False, drive=d["E"][None, :].copy(),
-                    desc=desc, flops_per_step=flops)
+                    desc=desc, flops_per_step=flops, n_total=n_inst)
     if name == "jc16":
         jc = W.jaynes_cummings()
         nt = nt or jc["nt"]
         bi = prepare_batch([jc["H"]], [jc["c_ops"]], [jc["rho0"]], [jc["e_ops"]])
         desc = dict(workload=name, n_inst=1, nt=nt, dt=jc["dt"], N=16, K=2)
+        # one instance: every rank runs a replica
         return dict(bi=bi, nt=nt, dt=jc["dt"], obs_t0=True, drive=None, desc=desc,
-                    flops_per_step=int(64 * 3 * 16 ** 3))
+                    flops_per_step=int(64 * 3 * 16 ** 3),
+                    n_total=1 if shard is None else shard[1])
     raise SystemExit("unknown workload %s" % name)
 
 
@@ -138,19 +146,56 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def run_gpu(args):
+def dist_context():
+    """One rank per GPU under torchrun (WORLD_SIZE > 1): the NCCL process group
+    serves only the barriers and the max-over-ranks of the timings; the
+    instances shard with no exchange on the data path."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return dict(rank=rank, world=world, local=local)
+
+
+def _max_over_ranks(ctx, values, dev):
+    """Element-wise max over ranks of a list of floats (identity on one GPU)."""
+    if ctx is None:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.cpu().tolist()
+
+
+def _barrier(ctx):
+    if ctx is not None:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_gpu(args, ctx=None):
     import torch
     from pyqed_gb300.build import build
     from pyqed_gb300.engine import Propagator
     build()
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", 0 if ctx is None else ctx["local"])
     torch.cuda.set_device(dev)
-    wl = make_workload(args.workload, args.n_inst, args.nt)
+    world = 1 if ctx is None else ctx["world"]
+    rank0 = ctx is None or ctx["rank"] == 0
+    wl = make_workload(args.workload, args.n_inst, args.nt,
+                       shard=None if ctx is None else (ctx["rank"], world))
     bi, nt, dt = wl["bi"], wl["nt"], wl["dt"]
-    n_inst = int(bi.dims.size)
+    n_inst = int(bi.dims.size)        # this rank's instances
+    n_total = int(wl.get("n_total", n_inst))  # the whole job's
     chosen = args.precision
-    paths = [chosen] + ([] if args.no_plain or chosen == "fp32" else ["fp32"])
-    if chosen == "3xbf16" and not args.no_plain:
+    paths = [chosen] + ([] if args.no_plain or chosen == "fp32" or ctx is not None else ["fp32"])
+    if chosen == "3xbf16" and not args.no_plain and ctx is None:
         paths.append("3xtf32")  # the other split precision, timed and checked beside it
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -174,13 +219,15 @@ def run_gpu(args):
             prop.propagate_device(rho0_dev, drive_dev, out)
         torch.cuda.synchronize()
         prop.check_errors()
-        clocks = ClockSampler(0)
+        clocks = ClockSampler(dev.index)
         if prec == chosen:
             clocks.start()
         times = []
         t_wall0 = time.perf_counter()
         for _ in range(args.steps):
             flush.fill_(1.0)  # evict L2 between timed steps (untimed)
+            torch.cuda.synchronize()
+            _barrier(ctx)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -189,6 +236,7 @@ def run_gpu(args):
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
         wall = time.perf_counter() - t_wall0
+        times = _max_over_ranks(ctx, times, dev)
         clk = clocks.stop() if prec == chosen else None
         prop.check_errors()
         info = prop.info()
@@ -223,6 +271,8 @@ def run_gpu(args):
     e2e_times = []
     for _ in range(args.steps):
         flush.fill_(1.0)
+        torch.cuda.synchronize()
+        _barrier(ctx)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -232,9 +282,17 @@ def run_gpu(args):
         e2e_times.append(e0.elapsed_time(e1) / 1e3)
     prop.check_errors()
     prop.close()
+    e2e_times = _max_over_ranks(ctx, e2e_times, dev)
     e2e_t = float(np.mean(e2e_times))
+    if ctx is not None:
+        import torch.distributed as dist
+        t = torch.tensor([float(h2d), float(d2h)], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)  # bytes copied by all ranks
+        h2d, d2h = t.cpu().tolist()
+    if not rank0:
+        return
 
-    inst_steps = n_inst * nt
+    inst_steps = n_total * nt
     ch = results[chosen]
     flops_launch = wl["flops_per_step"] * nt
     achieved = flops_launch / ch["sec_per_step"] / 1e12
@@ -244,15 +302,17 @@ def run_gpu(args):
     except Exception:
         pass
     line = dict(
-        metric=METRIC, value=inst_steps / ch["sec_per_step"], unit=UNIT, n_gpus=1,
+        metric=METRIC, value=inst_steps / ch["sec_per_step"], unit=UNIT, n_gpus=world,
         steps=args.steps, warmup=args.warmup, ms_per_step=ch["sec_per_step"] * 1e3,
         higher_is_better=True, scaling="weak", vs_baseline=None,
         dtype={"fp32": "c64 (fp32)", "fp64": "c128 (fp64)", "3xtf32": "c64 via 3xTF32",
                "3xbf16": "c64 via 3xBF16"}[chosen],
         data="synthetic (seeded generators, pyqed_gb300/workloads.py)",
         config=dict(wl["desc"], path=chosen, schedule=ch["info"]["schedule"],
-                    l2="flushed between timed steps (256 MB write)"),
-        gpu_launches=args.steps * ch["info"]["launches"],
+                    l2="flushed between timed steps (256 MB write)",
+                    parallelism="single GPU" if ctx is None else
+                    "%d GPUs, instances sharded by N^3 (LPT), no exchange; max over ranks" % world),
+        gpu_launches=args.steps * ch["info"]["launches"] * world,
     )
     # roofline of the dominant kernel (the propagate launch)
     if chosen in ("3xtf32", "3xbf16"):
@@ -317,6 +377,9 @@ def run_gpu(args):
     if not args.no_cpu:
         line["cpu_baseline"], line["accuracy"] = cpu_baseline_and_accuracy(
             wl, results, args, chosen)
+        if line["accuracy"] and chosen in line["accuracy"]:
+            # the metric holds at |drho| <= 1e-5: say whether the chosen path met it
+            line["accuracy_ok"] = line["accuracy"][chosen]["ok"]
     print(json.dumps(line))
 
 
@@ -718,11 +781,18 @@ def cpu_baseline_and_accuracy(wl, results, args, chosen):
     if wl.get("ex") is not None and args.workload == "exciton4096":
         from oracle import lindblad_oracle as O
         ex = wl["ex"]
-        pick = _sample_indices(wl["bi"].dims, args.acc_sample)
-        # the largest instance too (N = 65: the tensor-core block plus SIMT border)
-        big = int(np.argmax(wl["bi"].dims))
+        dims = wl["bi"].dims
+        pick = _sample_indices(dims, args.acc_sample)
+        # at least one instance of every padding class of the tensor-core
+        # kernel (NP = 16, 32, 48, 64) and the largest (N = 65: the border)
+        for lo, hi in ((1, 16), (17, 32), (33, 48), (49, 64), (65, 65)):
+            cls = np.nonzero((dims >= lo) & (dims <= hi))[0]
+            if cls.size and not any(lo <= dims[b] <= hi for b in pick):
+                pick.append(int(cls[-1]))
+        big = int(np.argmax(dims))
         if big not in pick:
-            pick = sorted(pick + [big])
+            pick.append(big)
+        pick = sorted(pick)
         acc = {}
         refs = {b: O.propagate_diag_correlation(ex["H"][b], ex["mu"][b], ex["rho_g"][b],
                                                 ex["c_diag"][b], ex["dt"], wl["nt"],
@@ -736,6 +806,7 @@ def cpu_baseline_and_accuracy(wl, results, args, chosen):
                 got = r["rho"][r["off"][b]:r["off"][b + 1]].reshape(N, N)
                 rerr.append(np.abs(got - refs[b][1]).max())
             acc[prec] = dict(max_rel_err_C=float(max(errs)), max_abs_err_rho_final=float(max(rerr)),
+                             ok=bool(max(errs) <= 1e-5 and max(rerr) <= 1e-5),
                              instances=pick, nt=wl["nt"],
                              reference="complex128 oracle (pyqed/oqs.py:717-791 recurrence)")
     del multiprocessing
@@ -855,12 +926,19 @@ def main():
         build()
         print(json.dumps(dict(adjoint=measure_adjoint(args, torch.device("cuda", 0)))))
         return
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    if world > 1:
-        # independent replicas of the batch, one per GPU (instances shard with
-        # no exchange); rank 0 reports.  Not exercised on this single-GPU pool.
-        raise SystemExit("multi-GPU runs are not supported by this build")
-    run_gpu(args)
+    ctx = dist_context()
+    if ctx is not None:
+        # one rank per GPU, each propagating its share of the instances; the
+        # extra sections (adjoint, large N, Redfield, HEOM, spectral, CPU
+        # baseline) are single-GPU measurements
+        args.no_adjoint = args.no_large_n = args.no_redfield = args.no_heom = True
+        args.no_spectral = args.no_cpu = True
+    try:
+        run_gpu(args, ctx)
+    finally:
+        if ctx is not None:
+            import torch.distributed as dist
+            dist.destroy_process_group()
 
 
 if __name__ == "__main__":
