@@ -25,19 +25,10 @@
 // accumulator, and one commit.
 //
 // Each of the 512 threads owns a quarter of the columns of one TMEM lane (one
-// component of one row); it keeps rho and a Kahan compensation term in
-// registers, forms the next stage input of the RK4 step in Horner form (below)
-// with a Kahan-compensated final update, splits it into hi/lo and writes it
-// into the XM and X^T buffers.
-//
-// RK4 (pyqed/phys.py:1051-1064) in Horner form.  Within a step the generator
-// L is fixed (a static H, or H(t_{k+1}) frozen for the step, as
-// pyqed/oqs.py:1790-1796), so the classic map rho -> rho + h/6 (k1 + 2 k2 +
-// 2 k3 + k4) is exactly the degree-4 Taylor polynomial of hL applied to rho,
-// evaluated here as
-//   y1 = rho + h/4 L rho,  y2 = rho + h/3 L y1,  y3 = rho + h/2 L y2,
-//   rho' = rho + h L y3,
-// the same map with no RK4 sum to carry between stages.
+// component of one row); it keeps rho, the RK4 sum, a Kahan compensation term
+// and the stage input in registers, performs the RK4 stage combination
+// (pyqed/phys.py:1051-1064) with a Kahan-compensated final update, splits the
+// next stage input into hi/lo and writes it into the XM and X^T buffers.
 // With BF16 operands the diagonal of A stays out of the split products: its
 // entries are of order one (the site energies) and BF16 hi + lo holds them
 // only to ~2^-17 relative, which turns into a phase error growing with t.
@@ -101,6 +92,8 @@ struct TcShared {
   int next[2];
   float2 red[2][kMaxEops][kWarps];  // per-warp observable partials
   double chk[2][kWarps][3];         // per-warp check partials: Tr rho (re, im), max hermiticity deviation
+  double chk_run[2][4];             // check state of each group's instance: Tr rho0 (re, im), max drift, max deviation
+  int chk_flags[2];                 // bit 0: rho0 Hermitian (deviation checked), bit 1: tolerance exceeded
 };
 
 // N = 65 (static H): the 64 x 64 block runs on the tensor cores as above; the
@@ -118,7 +111,7 @@ struct TcShared {
 constexpr int kBorder = 65;  // border index 64 plus one (the corner is entry 64 of the row arrays)
 struct TcBorder {
   float2 bx[2][2][kBorder];   // stage input [buffer][0: column c_i, 1: row r_j and corner]
-  float2 rho[2][kBorder], nkc[2][kBorder];
+  float2 rho[2][kBorder], racc[2][kBorder], nkc[2][kBorder];
   float2 aB[kBorder], bB[kBorder];      // A[i][g], A[g][j] (entry 64: alpha)
   float2 dcol[kBorder], drow[kBorder];  // D[i][g], D[g][j]
   float2 t1[64], t3[64], t4[64];        // (A_M c)_i, (b^T M)_j, (conj(A_M) r)_j of the stage
@@ -319,7 +312,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   const long long wo = p.woff[b];
   const int E = p.n_eops;
   const bool diag = p.cops_kind == 2 && p.n_cops > 0;
-  const float dt = (float)p.dt;
+  const float half_dt = (float)(0.5 * p.dt), dt = (float)p.dt, sixth_dt = (float)(p.dt / 6.0);
 
   unsigned char* SA = smem + G::OFF_A;
   unsigned char* SXM = smem + G::OFF_XM;
@@ -489,7 +482,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   // ---- state: element jj of this thread is component .x (jj even) or .y (jj
   // odd) of pair jj / 2, so the RK4 arithmetic runs on packed FP32x2 pairs;
   // nkc holds the negated Kahan compensation.
-  float2 rho2[NPQ / 2], nkc2[NPQ / 2];
+  float2 rho2[NPQ / 2], racc2[NPQ / 2], nkc2[NPQ / 2];
   auto rho_at = [&](int jj) -> float { return (jj & 1) ? rho2[jj >> 1].y : rho2[jj >> 1].x; };
 
   // ---- observables Tr[O rho]: FP32 partials per thread and warp (pairwise
@@ -518,9 +511,6 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   // resolution is that of the split operands.  Thread 0 of the group keeps
   // the running maxima.
   const bool checking = p.check_tol > 0.0 && p.chk != nullptr;
-  double2 chk_tr0 = make_double2(0.0, 0.0);
-  bool chk_herm = false, chk_bad = false;
-  double chk_dtr = 0.0, chk_dh = 0.0;
   auto xt_at = [&](int r, int k) -> float {  // component of X^T row r, K index k (hi + lo)
     const uint32_t o = off_t<BF16, NP>(r, k);
     return (float)*reinterpret_cast<const ET*>(SXT + o) + (float)*reinterpret_cast<const ET*>(SXT + G::LVL_T + o);
@@ -575,15 +565,19 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       tr.y += sh.chk[grp][w][1];
       h = fmax(h, sh.chk[grp][w][2]);
     }
+    double* run = sh.chk_run[grp];
     if (initial) {
-      chk_tr0 = tr;
-      chk_herm = h <= p.check_tol;
+      run[0] = tr.x;
+      run[1] = tr.y;
+      run[2] = run[3] = 0.0;
+      sh.chk_flags[grp] = h <= p.check_tol ? 1 : 0;
     } else {
-      const double ex = tr.x - chk_tr0.x, ey = tr.y - chk_tr0.y;
+      const double ex = tr.x - run[0], ey = tr.y - run[1];
       const double dtr = sqrt(ex * ex + ey * ey);
-      chk_dtr = fmax(chk_dtr, dtr);
-      if (chk_herm) chk_dh = fmax(chk_dh, h);
-      chk_bad = chk_bad || !(dtr <= p.check_tol) || (chk_herm && !(h <= p.check_tol));
+      const bool herm = (sh.chk_flags[grp] & 1) != 0;
+      run[2] = fmax(run[2], dtr);
+      if (herm) run[3] = fmax(run[3], h);
+      if (!(dtr <= p.check_tol) || (herm && !(h <= p.check_tol))) sh.chk_flags[grp] |= 2;
     }
   };
 
@@ -694,6 +688,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         rho2[jj >> 1].y = (float)v;
       } else {
         rho2[jj >> 1].x = (float)v;
+        racc2[jj >> 1] = make_float2(0.f, 0.f);
         nkc2[jj >> 1] = make_float2(0.f, 0.f);
       }
     }
@@ -745,6 +740,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       const float2 v = make_float2((float)z.x, (float)z.y);
       bd->rho[sl][t] = v;
       bd->bx[0][sl][t] = v;
+      bd->racc[sl][t] = make_float2(0.f, 0.f);
       bd->nkc[sl][t] = make_float2(0.f, 0.f);
     }
     gsync<GR>(grp);
@@ -869,13 +865,18 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         }
         const float2 rh = bd->rho[sl][t];
         float2 xn;
-        if (stage < 3) {
-          const float h = (float)(p.dt / (4 - stage));  // the block's Horner coefficient
+        if (stage == 0) {
+          bd->racc[sl][t] = R;
+          xn = make_float2(fmaf(half_dt, R.x, rh.x), fmaf(half_dt, R.y, rh.y));
+        } else if (stage < 3) {
+          const float2 ra = bd->racc[sl][t];
+          bd->racc[sl][t] = make_float2(fmaf(2.f, R.x, ra.x), fmaf(2.f, R.y, ra.y));
+          const float h = stage == 2 ? dt : half_dt;
           xn = make_float2(fmaf(h, R.x, rh.x), fmaf(h, R.y, rh.y));
         } else {
-          // Kahan-compensated rho += h L y3, as the block
-          const float2 nk = bd->nkc[sl][t];
-          const float yx = fmaf(dt, R.x, nk.x), yy = fmaf(dt, R.y, nk.y);
+          // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4), as the block
+          const float2 ra = bd->racc[sl][t], nk = bd->nkc[sl][t];
+          const float yx = fmaf(sixth_dt, ra.x + R.x, nk.x), yy = fmaf(sixth_dt, ra.y + R.y, nk.y);
           const float tx = rh.x + yx, ty = rh.y + yy;
           bd->nkc[sl][t] = make_float2(yx - (tx - rh.x), yy - (ty - rh.y));
           xn = make_float2(tx, ty);
@@ -945,17 +946,15 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       }
       fence_after_sync();
       // RHS element R = (combined accumulator) + (D o X); stages 0-2 form the
-      // next Horner stage input, stage 3 applies the Kahan-compensated
+      // RK4 sum and the next stage input, stage 3 applies the Kahan-compensated
       // update.  Each group of 4 columns (never crossing a 16-block) is loaded
       // from TMEM, combined with the partner lane, updated and written straight
       // into the operand buffers of the next stage.
-      // Horner coefficient of the stage: y_{s+1} = rho + h/(4 - s) L y_s
-      const float cstf = stage == 3 ? dt : (float)(p.dt / (4 - stage));
-      const float2 cst2 = make_float2(cstf, cstf);
+      const float2 cst2 = make_float2(stage == 2 ? dt : half_dt, stage == 2 ? dt : half_dt);
       // MODE 0: no diagonal dissipator term in this warp, 1: pure dephasing
       // (diagonal real D) in a warp that holds diagonal elements, 2: general
-      // diagonal D.  STAGE 0 (stages 0-2) or 3.  Mode and stage are resolved
-      // outside the unrolled element loops.
+      // diagonal D.  STAGE 0, 1 (stages 1 and 2) or 3.  Mode and stage are
+      // resolved outside the unrolled element loops.
       auto epilogue = [&](auto mode_tag, auto stage_tag) {
         constexpr int MODE = decltype(mode_tag)::value;
         constexpr int STAGE = decltype(stage_tag)::value;
@@ -1016,11 +1015,15 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
               R.x = fmaf(u0, r0.x, fmaf(u1, r0.y, fmaf(u2, a0.x, fmaf(u3, a0.y, R.x))));
               R.y = fmaf(u0, r1.x, fmaf(u1, r1.y, fmaf(u2, a1.x, fmaf(u3, a1.y, R.y))));
             }
-            if constexpr (STAGE < 3) {
+            if constexpr (STAGE == 0) {
+              racc2[k] = R;
+              xn2[h] = __ffma2_rn(cst2, R, rho2[k]);
+            } else if constexpr (STAGE == 1) {
+              racc2[k] = __ffma2_rn(make_float2(2.f, 2.f), R, racc2[k]);
               xn2[h] = __ffma2_rn(cst2, R, rho2[k]);
             } else {
-              // Kahan-compensated rho += h L y3
-              const float2 y = __ffma2_rn(cst2, R, nkc2[k]);
+              // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4)
+              const float2 y = __ffma2_rn(make_float2(sixth_dt, sixth_dt), __fadd2_rn(racc2[k], R), nkc2[k]);
               const float2 t = __fadd2_rn(rho2[k], y);
               nkc2[k] = __ffma2_rn(__ffma2_rn(rho2[k], m1, t), m1, y);  // y - (t - rho)
               rho2[k] = t;
@@ -1053,6 +1056,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         }
       };
       using S0 = std::integral_constant<int, 0>;
+      using S1 = std::integral_constant<int, 1>;
       using S3 = std::integral_constant<int, 3>;
       const int mode = !diag ? 0 : (dfast ? (dwarp ? 1 : 0) : 2);
       auto by_mode = [&](auto stage_tag) {
@@ -1060,7 +1064,8 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         else if (mode == 1) epilogue(std::integral_constant<int, 1>{}, stage_tag);
         else epilogue(std::integral_constant<int, 2>{}, stage_tag);
       };
-      if (stage < 3) by_mode(S0{});
+      if (stage == 0) by_mode(S0{});
+      else if (stage < 3) by_mode(S1{});
       else by_mode(S3{});
       bcur ^= 1;
     }
@@ -1092,9 +1097,10 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   }
   if (nonfinite && tid == 0) p.err[b] = 4;  // LGB_ERR_NONFINITE
   if (checking && tid == 0) {
-    p.chk[2 * b] = chk_dtr;
-    p.chk[2 * b + 1] = chk_herm ? chk_dh : -1.0;
-    if (chk_bad && p.err[b] == 0) p.err[b] = 9;  // LGB_ERR_CHECK
+    const int fl = sh.chk_flags[grp];
+    p.chk[2 * b] = sh.chk_run[grp][2];
+    p.chk[2 * b + 1] = (fl & 1) ? sh.chk_run[grp][3] : -1.0;
+    if ((fl & 2) && p.err[b] == 0) p.err[b] = 9;  // LGB_ERR_CHECK
   }
   if (alive && p.rho_out != nullptr && i < N) {
     double2* dst = p.rho_out + p.off[b];

@@ -144,3 +144,53 @@ def test_adjoint_finite_differences_in_E(built):
         Em[k] -= eps
         fd = (J(Ep) - J(Em)) / (2 * eps)
         assert abs(gE[k] - fd) < RTOL * max(np.abs(gE).max(), 1e-8)
+
+
+def test_adjoint_driven_workload_n64_k2_checkpoints_45(built):
+    """The driven workload's own shape: N = 64, K = 2 collapse operators with
+    rates gamma_k in [0.005, 0.02], the smooth Gaussian-process pulse, dt =
+    0.01, checkpoints every 45 steps, and the loss against the trajectory of a
+    perturbed pulse E + dE.  200 of the 2000 steps (four full checkpoint
+    segments and a partial one) keep the float64 reference affordable;
+    gradients in E(t) and gamma_k against float64 autograd on two instances
+    and central differences of the FP64 oracle at a few samples."""
+    from oracle import lindblad_oracle as Orc
+    from pyqed_gb300.adjoint import DrivenBatch, DrivenObservables
+    nt = 200
+    d = W.driven_batch(n_inst=2, N=64, K=2, nt=nt)
+    n, dt = len(d["H0"]), d["dt"]
+    batch = DrivenBatch(d["H0"], [[m] for m in d["mu"]], d["L"], d["rho0"], [[o] for o in d["O"]],
+                        dt, nt, checkpoint_every=45, device="cuda")
+    # target: the observables of the perturbed pulse
+    target = batch.forward(d["E_target"][None, :], d["gamma"])[:, :, 0].detach().clone()
+    E = torch.tensor(d["E"][None, :], dtype=torch.float64, device="cuda", requires_grad=True)
+    gam = torch.tensor(d["gamma"], dtype=torch.float64, device="cuda", requires_grad=True)
+    obs = DrivenObservables.apply(E, gam, batch)
+    loss = (torch.abs(obs[:, :, 0] - target) ** 2).sum()
+    loss.backward()
+    Er = torch.tensor(d["E"], dtype=torch.float64, requires_grad=True)
+    gr = torch.tensor(d["gamma"], dtype=torch.float64, requires_grad=True)
+    lr = _torch_loss(d, Er, gr, target.cpu())
+    lr.backward()
+    assert abs(loss.item() - lr.item()) < 1e-4 * max(1e-12, abs(lr.item()))
+    gE, gEr = E.grad[0].cpu().numpy(), Er.grad.numpy()
+    assert np.abs(gE - gEr).max() < RTOL * np.abs(gEr).max()
+    gg, ggr = gam.grad.cpu().numpy(), gr.grad.numpy()
+    assert np.abs(gg - ggr).max() < RTOL * np.abs(ggr).max()
+    # central differences of the FP64 oracle (instance 0, the same loss)
+    tg = target[0].cpu().numpy()
+
+    def J(Ev, g0):
+        Ls = [np.sqrt(g0[k]) * d["L"][0][k] for k in range(2)]
+        o, _ = Orc.lindblad_driven([d["H0"][0], [d["mu"][0], Ev]], d["rho0"][0], Ls, [d["O"][0]],
+                                   Nt=nt, dt=dt, store_states=False)
+        return float(np.sum(np.abs(o[:, 0] - tg) ** 2))
+    gE0 = torch.autograd.grad((torch.abs(DrivenObservables.apply(E, gam, batch)[0, :, 0] - target[0]) ** 2).sum(),
+                              E)[0][0].cpu().numpy()
+    eps = 1e-4
+    for k in (3, 97, nt - 1):
+        Ep, Em = d["E"].copy(), d["E"].copy()
+        Ep[k] += eps
+        Em[k] -= eps
+        fd = (J(Ep, d["gamma"][0]) - J(Em, d["gamma"][0])) / (2 * eps)
+        assert abs(gE0[k] - fd) < 5 * RTOL * np.abs(gE0).max(), (k, gE0[k], fd)

@@ -61,10 +61,14 @@ def test_exciton_correlation(golden):
     ex = W.exciton_batch(indices=[int(i) for i in g["indices"]], nt=int(g["nt"]))
     for i, n in enumerate(g["dims"]):
         assert np.array_equal(ex["H"][i], g["H"][i, :n, :n])
-        c_dense = [np.diag(c) for c in ex["c_diag"][i]]
-        cor = O.correlation_2op_1t(ex["H"][i], ex["rho_g"][i], ex["mu"][i], ex["mu"][i], c_dense,
-                                   ex["dt"], ex["nt"])
-        assert np.abs(cor - g["cor"][i]).max() < TOL
+        if n <= 24:
+            # the literal dense restatement (n dense projector collapse operators,
+            # 5n products per RHS) on the smaller instances; the diagonal form
+            # below covers all of them
+            c_dense = [np.diag(c) for c in ex["c_diag"][i]]
+            cor = O.correlation_2op_1t(ex["H"][i], ex["rho_g"][i], ex["mu"][i], ex["mu"][i], c_dense,
+                                       ex["dt"], ex["nt"])
+            assert np.abs(cor - g["cor"][i]).max() < TOL
         cor_d = O.propagate_diag_correlation(ex["H"][i], ex["mu"][i], ex["rho_g"][i],
                                              ex["c_diag"][i], ex["dt"], ex["nt"])
         assert np.abs(cor_d - g["cor"][i]).max() < TOL
