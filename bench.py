@@ -146,6 +146,32 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def measure_tf32_peak(dev, n=8192, reps=5):
+    """Dense TF32 tensor-core rate on this GPU: cuBLAS FP32 GEMM with TF32
+    math (torch.matmul, 2 n^3 flops), best of ``reps``, TFLOP/s."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        a = torch.randn(n, n, device=dev)
+        b = torch.randn(n, n, device=dev)
+        c = a @ b
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            best = t if best is None else min(best, t)
+        del a, b, c
+        return 2.0 * n ** 3 / best / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 def dist_context():
     """One rank per GPU under torchrun (WORLD_SIZE > 1): the NCCL process group
     serves only the barriers and the max-over-ranks of the timings; the
@@ -315,10 +341,11 @@ def run_gpu(args, ctx=None):
         gpu_launches=args.steps * ch["info"]["launches"] * world,
     )
     # roofline of the dominant kernel (the propagate launch)
+    tf32_peak = measure_tf32_peak(dev) if ("3xtf32" in results) else None
     if chosen in ("3xtf32", "3xbf16"):
         pk = peaks.get("bf16_tflops", 1900.0)
         if chosen == "3xtf32":
-            pk = pk / 2.0
+            pk = tf32_peak
         traffic = None
         if args.workload == "exciton4096":
             # DRAM bytes per launch: operator/rho0 reads measured by ncu on a
@@ -337,8 +364,8 @@ def run_gpu(args, ctx=None):
                                 traffic_note="bytes per launch: ncu-measured reads scaled to the "
                                              "full batch + algorithmic writes (profiles/)",
                                 note="algorithmic 64*N^3 flops per instance-step; peak = "
-                                     + ("measured bf16 / 2 (TF32 rate)" if chosen == "3xtf32"
-                                        else "measured bf16"))
+                                     + ("the TF32 rate measured here (cuBLAS TF32 GEMM 8192^3)"
+                                        if chosen == "3xtf32" else "measured bf16 (MEASURED_PEAKS.json)"))
     else:
         clk_mhz = (ch["clocks"] or {}).get("sm_max_mhz") or 2070.0
         pk = 152 * 128 * 2 * clk_mhz * 1e6 / 1e12
@@ -358,6 +385,10 @@ def run_gpu(args, ctx=None):
                 value=inst_steps / a["sec_per_step"], ms_per_step=a["sec_per_step"] * 1e3,
                 speedup_over_plain=(results["fp32"]["sec_per_step"] / a["sec_per_step"]
                                     if "fp32" in results else None))
+            if alt == "3xtf32" and tf32_peak:
+                ach = wl["flops_per_step"] * nt / a["sec_per_step"] / 1e12
+                line["alternatives"][alt].update(achieved_tflops=ach, tf32_peak_measured=tf32_peak,
+                                                 frac=ach / tf32_peak)
     line["e2e"] = dict(value=inst_steps / e2e_t, unit=UNIT, ms_per_step=e2e_t * 1e3,
                        h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
                        api="pyqed_gb300.engine.Propagator.set_operators + propagate "
@@ -741,9 +772,13 @@ def _sample_indices(dims, count):
     return sorted(int(order[i]) for i in q)
 
 
-def cpu_port_rate(wl, n_sample, steps):
-    """Reference algorithm (dense RHS, pyqed/oqs.py:697-715 + pyqed/phys.py:1051-1064),
-    restated by the oracle, on a stratified sample of instances."""
+def cpu_port_rate(wl, n_sample, steps, csr=False):
+    """Reference algorithm (the RHS of pyqed/oqs.py:697-715 + the RK4 of
+    pyqed/phys.py:1051-1064), restated by the oracle, on a stratified sample
+    of instances: dense numpy complex128 as ``_fast_lindblad``
+    (pyqed/oqs.py:1492-1594) computes it, or with ``csr`` on scipy.sparse
+    CSR operators and state as the reference's public ``run`` (``_lindblad``,
+    pyqed/oqs.py:1596-1696) does."""
     from oracle import lindblad_oracle as O
     bi = wl["bi"]
     dims = bi.dims
@@ -763,6 +798,10 @@ def cpu_port_rate(wl, n_sample, steps):
         else:
             cops = []
         rho = bi.rho0[off[b]:off[b + 1]].reshape(N, N).copy()
+        if csr:
+            from scipy.sparse import csr_matrix
+            H, rho = csr_matrix(H), csr_matrix(rho)
+            cops = [csr_matrix(c) for c in cops]
         t0 = time.perf_counter()
         for _ in range(steps):
             rho = O.rk4_step(rho, wl["dt"], H, cops)
@@ -777,10 +816,15 @@ def cpu_baseline_and_accuracy(wl, results, args, chosen):
     import multiprocessing
     cores = os.cpu_count() or 1
     rate, idx = cpu_port_rate(wl, args.cpu_sample, args.cpu_steps)
+    rate_csr, _ = cpu_port_rate(wl, args.cpu_sample, max(1, args.cpu_steps // 2), csr=True)
     cb = dict(value=rate, unit=UNIT, cores=cores, kind="port",
               sample="%d instances stratified by N x %d RK4 steps, dense numpy complex128 "
-                     "(oracle restatement of the reference's RHS + rk4, BLAS threads = host)"
-                     % (len(idx), args.cpu_steps))
+                     "(oracle restatement of the reference's RHS + rk4 as _fast_lindblad computes "
+                     "it, BLAS threads = host)" % (len(idx), args.cpu_steps),
+              csr_value=rate_csr,
+              csr_sample="the same instances x %d steps with scipy.sparse CSR operators and state, "
+                         "as the reference's public run (single-threaded scipy)"
+                         % max(1, args.cpu_steps // 2))
     acc = None
     if wl.get("ex") is not None and args.workload == "exciton4096":
         from oracle import lindblad_oracle as O
@@ -864,7 +908,7 @@ def main():
     ap.add_argument("--nt", type=int, default=None)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-sample", type=int, default=16)
+    ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--acc-sample", type=int, default=4)
     ap.add_argument("--no-adjoint", action="store_true")
