@@ -29,13 +29,14 @@
 // and the stage input in registers, performs the RK4 stage combination
 // (pyqed/phys.py:1051-1064) with a Kahan-compensated final update, splits the
 // next stage input into hi/lo and writes it into the XM and X^T buffers.
-// With BF16 operands the diagonal of A stays out of the split products: its
-// entries are of order one (the site energies) and BF16 hi + lo holds them
-// only to ~2^-17 relative, which turns into a phase error growing with t.
-// Its term (a_i + conj(a_j)) X_ij is formed in FP32 from the FP32 stage input
-// and written into the part-0 accumulator columns (part-1 columns zeroed)
-// before the stage's MMAs, which accumulate onto it; the off-diagonal
-// couplings are small, so their BF16 representation error is too.
+// The diagonal of A stays out of the split products: its entries are of
+// order one (the site energies) and a hi + lo split holds them only to
+// ~2^-17 (BF16) or ~2^-21 (TF32) relative, which turns into a phase error
+// growing with t.  Its term (a_i + conj(a_j)) X_ij is formed in FP32 from the
+// FP32 stage input and written into the part-0 accumulator columns (part-1
+// columns zeroed) before the stage's MMAs, which accumulate onto it; the
+// off-diagonal couplings are small, so their split representation error is
+// too.
 // Observables Tr[O rho] (pyqed/phys.py:1257-1264) of step k are reduced while
 // the tensor core runs the first stage of step k + 1.  Every mbarrier wait is
 // bounded; a wait that runs out marks the instance LGB_ERR_TIMEOUT and the CTA
@@ -86,7 +87,7 @@ template <> struct Elem<true> {
 // Two thread groups (the warps of TMEM lane quarters 0-1 and 2-3) run separate
 // instances when NP <= 32; otherwise group 0 is the whole CTA.
 struct TcShared {
-  alignas(16) float2 adg[2][64];  // BF16: diagonal of A of each group's instance
+  alignas(16) float2 adg[2][64];  // diagonal of A of each group's instance (applied in FP32)
   uint64_t mbar[2];
   uint32_t tmem_base;
   int next[2];
@@ -115,18 +116,25 @@ struct TcBorder {
   float2 aB[kBorder], bB[kBorder];      // A[i][g], A[g][j] (entry 64: alpha)
   float2 dcol[kBorder], drow[kBorder];  // D[i][g], D[g][j]
   float2 t1[64], t3[64], t4[64];        // (A_M c)_i, (b^T M)_j, (conj(A_M) r)_j of the stage
+  float2 t3p[2][64];                    // BF16: b^T M_p of the real (p = 0) and imaginary parts
   float2 t2p[2][64][4];                 // (M conj(b))_i partials of the four column groups, per bx buffer
   float2 csum[2];                       // corner sums b.c and r.conj(b)
 };
 
-// Shared-memory geometry of one instance.  All operands are K-major with
-// core matrices of 8 rows x 16 bytes.
-//   "S" layout (A buffer, XM buffer): the K-direction core matrices of an
-//   8-row group are adjacent (LBO 128 B), row groups SBO_S apart;
-//   "T" layout (X^T buffer): K-direction core matrices 144 B apart and row
-//   groups SBO_T apart, SBO_T = 32 mod 64 B, so that the column-wise scalar
-//   stores of a warp (16 rows i of each of two row halves, 2 row groups
-//   apart) hit distinct banks.
+// Shared-memory geometry of one instance.  Core matrices of 8 rows x 16 bytes.
+//   "S" layout (A buffer, XM buffer), K-major: the K-direction core matrices
+//   of an 8-row group are adjacent (LBO 128 B), row groups SBO_S apart;
+//   X^T buffer (the N side of A X), TF32: the K-major "T" layout, K-direction
+//   core matrices 144 B apart and row groups SBO_T apart, SBO_T = 32 mod
+//   64 B, so that the column-wise scalar stores of a warp (16 rows i of each
+//   of two row halves, 2 row groups apart) hit distinct banks;
+//   X^T buffer, BF16: MN-major (the instruction descriptor's transpose-B
+//   bit), i.e. X's own rows: core matrices of 8 K-rows (i) x 8 N-elements
+//   (j), N-direction ones adjacent (SBO 128 B), K-direction ones SK_M apart
+//   (LBO).  A thread's four columns of row i are then one 8-byte piece of a
+//   core-matrix row (16 bytes for two groups) instead of four scalars.  The
+//   descriptor reading (LBO = the K-direction stride for MN-major operands)
+//   was checked by an in-bounds probe against a CPU product.
 // Each buffer holds the hi level (2 NP rows) followed by the lo level.  An
 // M-side operand reads 128 rows from its level base; the rows past 2 NP belong
 // to lanes no thread uses and stay inside the buffer (BYTES covers the last
@@ -138,10 +146,15 @@ struct Geo {
   static constexpr uint32_t LVL_S = (2 * NP / 8) * SBO_S;
   static constexpr uint32_t LBO_T = 144;
   static constexpr uint32_t SBO_T = (NP / EPC) * 144 + (96u - ((NP / EPC) * 144u) % 64u) % 64u;
-  static constexpr uint32_t LVL_T = (2 * NP / 8) * SBO_T;
+  // BF16: the X^T buffer is the MN-major B operand instead: element (n, k)
+  // at (n / 8) SN_M + (k / 8) SK_M + (k % 8) 16 + (n % 8) 2, core matrices of
+  // 8 K-rows x 8 N-elements, N-direction ones adjacent
+  static constexpr uint32_t SN_M = 128;
+  static constexpr uint32_t SK_M = (2 * NP / 8) * 128;
+  static constexpr uint32_t LVL_T = BF16 ? (NP / 8) * SK_M : (2 * NP / 8) * SBO_T;
   static constexpr int KS = NP / Elem<BF16>::kK;  // MMA K-steps
   static constexpr uint32_t KSTEP_S = (Elem<BF16>::kK / EPC) * 128;
-  static constexpr uint32_t KSTEP_T = (Elem<BF16>::kK / EPC) * LBO_T;
+  static constexpr uint32_t KSTEP_T = BF16 ? 2 * SK_M : (Elem<BF16>::kK / EPC) * LBO_T;
   static constexpr uint32_t OFF_A = 0;
   static constexpr uint32_t OFF_XM = 2 * LVL_S;
   static constexpr uint32_t OFF_XT = 4 * LVL_S;
@@ -162,12 +175,18 @@ __device__ __forceinline__ uint32_t off_s(int r, int k) {
   return (uint32_t)(r >> 3) * G::SBO_S + (uint32_t)(k / G::EPC) * 128u + (uint32_t)(r & 7) * 16u +
          (uint32_t)(k % G::EPC) * Elem<BF16>::kSize;
 }
-// Byte offset of element (r, k) in the T layout.
+// Byte offset of element (r, k) of the X^T buffer (N row r, K index k): the
+// T layout (TF32), the MN-major layout (BF16).
 template <bool BF16, int NP>
 __device__ __forceinline__ uint32_t off_t(int r, int k) {
   using G = Geo<BF16, NP>;
-  return (uint32_t)(r >> 3) * G::SBO_T + (uint32_t)(k / G::EPC) * G::LBO_T + (uint32_t)(r & 7) * 16u +
-         (uint32_t)(k % G::EPC) * Elem<BF16>::kSize;
+  if constexpr (BF16) {
+    return (uint32_t)(r >> 3) * G::SN_M + (uint32_t)(k >> 3) * G::SK_M + (uint32_t)(k & 7) * 16u +
+           (uint32_t)(r & 7) * 2u;
+  } else {
+    return (uint32_t)(r >> 3) * G::SBO_T + (uint32_t)(k / G::EPC) * G::LBO_T + (uint32_t)(r & 7) * 16u +
+           (uint32_t)(k % G::EPC) * Elem<BF16>::kSize;
+  }
 }
 
 template <bool BF16>
@@ -193,21 +212,23 @@ template <bool BF16, int NP>
 __device__ __forceinline__ void issue_stage(uint32_t d, uint32_t base, uint32_t mshift) {
   using G = Geo<BF16, NP>;
   constexpr uint32_t id = idesc(Elem<BF16>::kFmt, 128, 2 * NP, false, false);
+  constexpr uint32_t idx = idesc(Elem<BF16>::kFmt, 128, 2 * NP, false, BF16);  // A X: B MN-major (BF16)
   const uint64_t dAm = sdesc(base + G::OFF_A - mshift, 128, G::SBO_S);  // A as M side
   const uint64_t dAn = sdesc(base + G::OFF_A, 128, G::SBO_S);           // A as N side
   const uint64_t dXM = sdesc(base + G::OFF_XM - mshift, 128, G::SBO_S);
-  const uint64_t dXT = sdesc(base + G::OFF_XT, G::LBO_T, G::SBO_T);
+  const uint64_t dXT = BF16 ? sdesc(base + G::OFF_XT, G::SK_M, G::SN_M)
+                            : sdesc(base + G::OFF_XT, G::LBO_T, G::SBO_T);
   // A X: A_hi X_hi, A_hi X_lo, A_lo X_hi
-  // (BF16: the accumulator already holds the diagonal term, so every MMA accumulates)
+  // (the accumulator already holds the diagonal term, so every MMA accumulates)
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, (BF16 || s > 0) ? 1u : 0u);
+    mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), idx, 1u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, G::LVL_T + s * G::KSTEP_T), id, 1u);
+    mma<BF16>(d, dadd(dAm, s * G::KSTEP_S), dadd(dXT, G::LVL_T + s * G::KSTEP_T), idx, 1u);
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
-    mma<BF16>(d, dadd(dAm, G::LVL_S + s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), id, 1u);
+    mma<BF16>(d, dadd(dAm, G::LVL_S + s * G::KSTEP_S), dadd(dXT, s * G::KSTEP_T), idx, 1u);
   // X A^dag = (-i X) (i A^dag): X_hi A_hi, X_hi A_lo, X_lo A_hi
 #pragma unroll
   for (int s = 0; s < G::KS; ++s)
@@ -344,11 +365,9 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
             a.y = fmaf(f[d], g.y, a.y);
           }
       }
-      if constexpr (BF16) {
-        if (k == r) {  // applied in FP32 by inject
-          sh.adg[grp][r] = a;
-          a = make_float2(0.f, 0.f);
-        }
+      if (k == r) {  // applied in FP32 by inject
+        sh.adg[grp][r] = a;
+        a = make_float2(0.f, 0.f);
       }
       float h, lo;
       El::split(a.x, h, lo);
@@ -390,19 +409,8 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         h[q] = *reinterpret_cast<const uint32_t*>(&hb);
         l[q] = *reinterpret_cast<const uint32_t*>(&lb);
       }
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const uint32_t o = off_t<BF16, NP>(ncol(c, col + e), i);
-        const int sh16 = (e & 1) * 16;
-        *reinterpret_cast<uint16_t*>(SXT + o) = (uint16_t)(h[e >> 1] >> sh16);
-        *reinterpret_cast<uint16_t*>(SXT + G::LVL_T + o) = (uint16_t)(l[e >> 1] >> sh16);
-      }
-      // -bf16(x) = bf16(-x) exactly: the XM sign is a flip of the sign bits
-#pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        h[q] ^= xm_flip;
-        l[q] ^= xm_flip;
-      }
+      // X^T (MN-major): the 4 columns are 4 consecutive N elements of K-row i
+      // (one 8-byte piece of a core-matrix row; 16 bytes for a pair of groups)
       if constexpr (kXmPairs) {
         if ((g & 1) == 0) {
           xph[0] = h[0];
@@ -410,13 +418,23 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
           xpl[0] = l[0];
           xpl[1] = l[1];
         } else {
-          *reinterpret_cast<uint4*>(SXM + off_s<BF16, NP>(xm_row, col - 4)) = make_uint4(xph[0], xph[1], h[0], h[1]);
-          *reinterpret_cast<uint4*>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col - 4)) =
-              make_uint4(xpl[0], xpl[1], l[0], l[1]);
+          const uint32_t o = off_t<BF16, NP>(ncol(c, col - 4), i);
+          *reinterpret_cast<uint4*>(SXT + o) = make_uint4(xph[0], xph[1], h[0], h[1]);
+          *reinterpret_cast<uint4*>(SXT + G::LVL_T + o) = make_uint4(xpl[0], xpl[1], l[0], l[1]);
+          // -bf16(x) = bf16(-x) exactly: the XM sign is a flip of the sign bits
+          const uint32_t m = off_s<BF16, NP>(xm_row, col - 4);
+          *reinterpret_cast<uint4*>(SXM + m) =
+              make_uint4(xph[0] ^ xm_flip, xph[1] ^ xm_flip, h[0] ^ xm_flip, h[1] ^ xm_flip);
+          *reinterpret_cast<uint4*>(SXM + G::LVL_S + m) =
+              make_uint4(xpl[0] ^ xm_flip, xpl[1] ^ xm_flip, l[0] ^ xm_flip, l[1] ^ xm_flip);
         }
       } else {
-        *reinterpret_cast<uint2*>(SXM + off_s<BF16, NP>(xm_row, col)) = make_uint2(h[0], h[1]);
-        *reinterpret_cast<uint2*>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col)) = make_uint2(l[0], l[1]);
+        const uint32_t o = off_t<BF16, NP>(ncol(c, col), i);
+        *reinterpret_cast<uint2*>(SXT + o) = make_uint2(h[0], h[1]);
+        *reinterpret_cast<uint2*>(SXT + G::LVL_T + o) = make_uint2(l[0], l[1]);
+        const uint32_t m = off_s<BF16, NP>(xm_row, col);
+        *reinterpret_cast<uint2*>(SXM + m) = make_uint2(h[0] ^ xm_flip, h[1] ^ xm_flip);
+        *reinterpret_cast<uint2*>(SXM + G::LVL_S + m) = make_uint2(l[0] ^ xm_flip, l[1] ^ xm_flip);
       }
     } else {
       float vh[4], vl[4];
@@ -434,14 +452,14 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       st4<BF16>(SXM + G::LVL_S + off_s<BF16, NP>(xm_row, col), vl);
     }
   };
-  // BF16: the diagonal term (a_i + conj(a_j)) X_ij of the stage input x
-  // (columns j0 + 4g .. + 3; the partner lane holds the other component) into
-  // the part-0 accumulator columns, the part-1 columns zeroed.  Warp-uniform.
+  // The diagonal term (a_i + conj(a_j)) X_ij of the stage input x (columns
+  // j0 + 4g .. + 3; the partner lane holds the other component) into the
+  // part-0 accumulator columns, the part-1 columns zeroed.  Warp-uniform.
   const float sgx = c == 0 ? -1.f : 1.f;
   // ai: a_i of this thread's row (adg_row())
   auto adg_row = [&]() -> float2 { return row_ok ? sh.adg[grp][i] : make_float2(0.f, 0.f); };
   auto inject = [&](int g, const float* x4, float2 ai) {
-    if constexpr (BF16) {
+    {
       const int col = j0 + g * 4;
       float q[4];
 #pragma unroll
@@ -787,7 +805,42 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         sy += __shfl_xor_sync(0xffffffffu, sy, 2);
         if (q == 0) (t4 ? bd->t4 : bd->t1)[row] = make_float2(sx, sy);
       }
-      {  // (b^T M)_j from the X^T operand (hi + lo): eight threads per column, 8 k each
+      if constexpr (BF16) {
+        // (b^T M)_j from the MN-major X^T operand (hi + lo): warp w takes
+        // N-group w (8 consecutive n, one part p of 8 columns j) and walks the
+        // eight K-groups; lane l reads K-row l >> 2, N pair 2 (l & 3), so that
+        // each load of the warp is one 128-byte core matrix.  The partial sums
+        // over k meet across the eight lanes of an N pair.
+        const int ng = warp;
+        const int p_part = (ng & 3) < 2 ? 1 : 0;  // ncol: the odd 16-block holds part 0
+        const int jbase = 16 * (ng >> 2) + 8 * (ng & 1);
+        const int kr = lane >> 2, np2 = 2 * (lane & 3);
+        float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f;  // b_k M_p[k][j], j = jbase + np2 + {0, 1}
+#pragma unroll
+        for (int kg = 0; kg < NP / 8; ++kg) {
+          const int k = kg * 8 + kr;
+          const uint32_t o = (uint32_t)ng * G::SN_M + (uint32_t)kg * G::SK_M + (uint32_t)kr * 16u + (uint32_t)np2 * 2u;
+          const __nv_bfloat162 hv = *reinterpret_cast<const __nv_bfloat162*>(SXT + o);
+          const __nv_bfloat162 lv = *reinterpret_cast<const __nv_bfloat162*>(SXT + G::LVL_T + o);
+          const float2 m = __fadd2_rn(__bfloat1622float2(hv), __bfloat1622float2(lv));
+          const float2 bk = bd->bB[k];
+          s0x = fmaf(bk.x, m.x, s0x);
+          s0y = fmaf(bk.y, m.x, s0y);
+          s1x = fmaf(bk.x, m.y, s1x);
+          s1y = fmaf(bk.y, m.y, s1y);
+        }
+#pragma unroll
+        for (int o = 4; o < 32; o <<= 1) {
+          s0x += __shfl_xor_sync(0xffffffffu, s0x, o);
+          s0y += __shfl_xor_sync(0xffffffffu, s0y, o);
+          s1x += __shfl_xor_sync(0xffffffffu, s1x, o);
+          s1y += __shfl_xor_sync(0xffffffffu, s1y, o);
+        }
+        if (kr == 0) {
+          bd->t3p[p_part][jbase + np2] = make_float2(s0x, s0y);
+          bd->t3p[p_part][jbase + np2 + 1] = make_float2(s1x, s1y);
+        }
+      } else {  // (b^T M)_j from the X^T operand (hi + lo): eight threads per column, 8 k each
         const int j = tid >> 3, q = tid & 7;
         const int rr = ncol(0, j), ri = ncol(1, j);
         float sx = 0.f, sy = 0.f;
@@ -849,7 +902,12 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
           cmac(R, bd->dcol[t], x);
         } else if (t < kG) {
           const float2 x = br[t], a = bd->aB[t];
-          R = bd->t3[t];
+          if constexpr (BF16) {  // b^T M = b^T M_0 + i b^T M_1
+            const float2 u = bd->t3p[0][t], v = bd->t3p[1][t];
+            R = make_float2(u.x - v.y, u.y + v.x);
+          } else {
+            R = bd->t3[t];
+          }
           R.x += bd->t4[t].x;
           R.y += bd->t4[t].y;
           cmac(R, al, x);
@@ -909,7 +967,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
       for (int d = 0; d < 4; ++d) f[d] = (d < p.n_drive) ? (float)drv[(long long)d * p.nt + step] : 0.f;
       build_a(f);
     }
-    if constexpr (BF16) {
+    {
       // diagonal term of the first stage (later steps of a static H get it from
       // the last epilogue of the step before)
       if (step == 0 || p.n_drive > 0) {
@@ -967,7 +1025,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
         [[maybe_unused]] float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f, tx = 0.f, ty = 0.f;
         [[maybe_unused]] const float2* brow = nullptr;
         [[maybe_unused]] float2 ai_row = make_float2(0.f, 0.f);
-        if constexpr (BF16) ai_row = adg_row();
+        ai_row = adg_row();
         if constexpr (BD) {
           const float2 ai = bd->aB[i], ci = bd->bx[bcur][0][i];
           u0 = c == 0 ? ai.x : ai.y;
@@ -1044,11 +1102,9 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
           }
           const float x4[4] = {xn2[0].x, xn2[0].y, xn2[1].x, xn2[1].y};
           write_group(g, x4);
-          if constexpr (BF16) {
-            if (STAGE < 3 || p.n_drive == 0) inject(g, x4, ai_row);
-          }
+          if (STAGE < 3 || p.n_drive == 0) inject(g, x4, ai_row);
         }
-        if constexpr (BF16) tmem_wait_st();
+        tmem_wait_st();
         if constexpr (BD) {
           tx += __shfl_xor_sync(0xffffffffu, tx, 16);
           ty += __shfl_xor_sync(0xffffffffu, ty, 16);
