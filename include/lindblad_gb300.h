@@ -199,6 +199,11 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
  *                      kernel skip its first MMA commit, so that its bounded
  *                      wait (4096 polls) runs out and every instance it was
  *                      given reports LGB_ERR_TIMEOUT; nothing faults or hangs
+ *   LGB_OPT_GEMM_KSPLIT split-precision GEMM schedule: cap on the split-K
+ *                      factors (0: none, else a power of two <= 64)
+ *   LGB_OPT_GRAPH_STEPS GEMM schedule: RK4 steps captured per CUDA graph
+ *                      (1..64, default 16; propagations of fewer than two
+ *                      graphs' worth of steps launch directly)
  *   LGB_OPT_CHECK      per-step check of the state, accumulated in FP64:
  *                      0 (default) off; v = 1..15 checks after every step
  *                      that |Tr rho(t) - Tr rho0| <= 10^-v and, for
@@ -216,7 +221,9 @@ typedef enum {
   LGB_OPT_TC_PAIRS = 1,
   LGB_OPT_GEMM_WAVES = 2,
   LGB_OPT_TEST_STALL = 3,
-  LGB_OPT_CHECK = 4
+  LGB_OPT_CHECK = 4,
+  LGB_OPT_GEMM_KSPLIT = 5,
+  LGB_OPT_GRAPH_STEPS = 6
 } lgb_option_t;
 
 int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value);

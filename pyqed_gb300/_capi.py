@@ -49,7 +49,8 @@ EXPORTS = [
     "lgb_spectral_sum", "lgb_spectral_2t",
 ]
 # tuning options (lgb_option_t)
-OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3, "check": 4}
+OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3, "check": 4, "gemm_ksplit": 5,
+       "graph_steps": 6}
 FLAG_ADJOINT = 1
 HEOM_DOUBLE_FIRST = 1
 HEOM_DIAG_SZ = 2

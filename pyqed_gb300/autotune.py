@@ -3,8 +3,9 @@
 The library picks a schedule by rule (instances that fit one CTA run on the
 CTA-resident / tensor-core kernels, larger ones on the grid-wide GEMM
 schedule) and exposes tuning options (``lgb_plan_set_option``: two
-instances per CTA on the tensor cores for NP <= 32, one or two waves of
-split-K CTAs in the split-precision GEMM schedule).  ``tune`` times every
+instances per CTA on the tensor cores for NP <= 32; for the GEMM schedule
+the RK4 steps per captured CUDA graph, and for its split precisions one or
+two waves of split-K CTAs and a cap on the split-K factor).  ``tune`` times every
 valid candidate on the caller's own operators for a few RK4 steps (CUDA
 events, after one untimed run) and returns the fastest; results are cached
 per problem signature and GPU in a JSON file (``$PYQED_GB300_TUNE_CACHE``,
@@ -62,9 +63,15 @@ def candidates(dims, precision, cops_kind, n_cops, n_drive=0):
     if precision == "3xbf16" and fits_tc:
         return out
     if dims.size <= _GEMM_MAX_INST:
-        out.append(dict(schedule="gemm", options={}))
-        if split:
-            out.append(dict(schedule="gemm", options={"gemm_waves": 2}))
+        # the GEMM schedule: steps per captured CUDA graph, and for the split
+        # precisions the split-K shape (waves of CTAs, a cap on the factor)
+        for gs in (16, 32):
+            base = {} if gs == 16 else {"graph_steps": gs}
+            out.append(dict(schedule="gemm", options=dict(base)))
+            if split:
+                out.append(dict(schedule="gemm", options=dict(base, gemm_waves=2)))
+                for cap in (4, 8):
+                    out.append(dict(schedule="gemm", options=dict(base, gemm_ksplit=cap)))
     return out
 
 
@@ -91,7 +98,7 @@ def _time_candidate(cand, make_prop, operators, rho0, drive, reps):
     import torch
     from . import _capi as C
     try:
-        prop = make_prop(cand["schedule"])
+        prop = make_prop(cand)
     except C.LindbladError as e:
         if e.status == 2:  # LGB_ERR_UNSUPPORTED: not a valid schedule for this problem
             return None
@@ -144,20 +151,29 @@ def tune(bi, *, dt, precision, obs_t0=False, drive=None, drive_shared=True, devi
     if timer is None:
         from .engine import Propagator
 
-        def make_prop(schedule):
-            return Propagator(bi.dims, nt=nt_probe, dt=dt, n_cops=bi.n_cops, cops_kind=bi.cops_kind,
+        def probe_steps(c):
+            # GEMM candidates run two captured graphs' worth of steps, so that
+            # the graph length is part of what is timed
+            return max(nt_probe, 2 * c["options"].get("graph_steps", 16)) if c["schedule"] == "gemm" else nt_probe
+
+        def make_prop(c):
+            return Propagator(bi.dims, nt=probe_steps(c), dt=dt, n_cops=bi.n_cops, cops_kind=bi.cops_kind,
                               n_eops=bi.n_eops, n_drive=bi.n_drive, obs_t0=obs_t0,
-                              precision=precision, schedule=schedule, drive_shared=drive_shared,
+                              precision=precision, schedule=c["schedule"], drive_shared=drive_shared,
                               device=device)
-        drive_probe = None
-        if bi.n_drive:
-            drive_probe = np.asarray(drive, dtype=np.float64)
-            drive_probe = drive_probe[..., :nt_probe] if drive_probe.shape[-1] >= nt_probe else \
-                np.pad(drive_probe, [(0, 0)] * (drive_probe.ndim - 1) + [(0, nt_probe - drive_probe.shape[-1])])
+
+        def drive_for(nsteps):
+            if not bi.n_drive:
+                return None
+            d = np.asarray(drive, dtype=np.float64)
+            return d[..., :nsteps] if d.shape[-1] >= nsteps else \
+                np.pad(d, [(0, 0)] * (d.ndim - 1) + [(0, nsteps - d.shape[-1])])
         ops = (bi.H, bi.cops, bi.eops, bi.dops)
 
         def timer(c):  # noqa: F811
-            return _time_candidate(c, make_prop, ops, bi.rho0, drive_probe, reps)
+            ms = _time_candidate(c, make_prop, ops, bi.rho0, drive_for(probe_steps(c)), reps)
+            # per probe step, so that candidates with different probe lengths compare
+            return None if ms is None else ms / probe_steps(c)
     timings = []
     for c in cands:
         t = timer(c)

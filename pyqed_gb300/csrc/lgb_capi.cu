@@ -526,6 +526,7 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
       a.obs_out = p.obs_out ? p.obs_out + (long long)b * nrows * pr.n_eops : nullptr;
       a.rho_out = p.rho_out ? p.rho_out + plan->off[b] : nullptr;
       a.states_out = p.states_out ? p.states_out + plan->soff[b] : nullptr;
+      a.graph_steps = plan->opt_gsteps;
       a.check_tol = p.check_tol;
       a.chk = plan->d_chk + 2 * b;
       a.chk_ws = plan->d_chkws + 8 * b;
@@ -711,9 +712,20 @@ int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value) {
       if (value != 1 && value != 2) return LGB_ERR_INVALID_ARG;
       plan->opt_waves = value;
       const int Kd = plan->prob.cops_kind == LGB_COPS_DENSE ? plan->prob.n_cops : 0;
-      for (auto& q : plan->gsplit) lgb::split_set_ksplit(q, Kd, plan->n_sm * value);
+      for (auto& q : plan->gsplit) lgb::split_set_ksplit(q, Kd, plan->n_sm * value, plan->opt_kcap);
       return LGB_OK;
     }
+    case LGB_OPT_GEMM_KSPLIT: {
+      if (value != 0 && (value < 1 || value > 64 || (value & (value - 1)) != 0)) return LGB_ERR_INVALID_ARG;
+      plan->opt_kcap = value;
+      const int Kd = plan->prob.cops_kind == LGB_COPS_DENSE ? plan->prob.n_cops : 0;
+      for (auto& q : plan->gsplit) lgb::split_set_ksplit(q, Kd, plan->n_sm * plan->opt_waves, value);
+      return LGB_OK;
+    }
+    case LGB_OPT_GRAPH_STEPS:
+      if (value < 1 || value > 64) return LGB_ERR_INVALID_ARG;
+      plan->opt_gsteps = value;
+      return LGB_OK;
     case LGB_OPT_TEST_STALL:
       if (value != 0 && value != 1) return LGB_ERR_INVALID_ARG;
       plan->opt_stall = value;

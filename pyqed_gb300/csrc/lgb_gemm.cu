@@ -473,7 +473,7 @@ static int gemm_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
     step_inc_kernel<<<1, 1, 0, s>>>(a.ctr);
     return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
   };
-  const int r = run_steps(a.nt, st, a.cap, one_step);
+  const int r = run_steps(a.nt, st, a.cap, one_step, a.graph_steps);
   cublasSetStream(a.blas, st);
   if (r != LGB_OK) return r;
   if (a.nt == 0 && a.rho_out != nullptr)

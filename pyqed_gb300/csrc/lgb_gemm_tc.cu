@@ -531,9 +531,10 @@ bool make_map(CUtensorMap* m, void* base, bool bf16, long long rows, long long p
 
 // K-dimension split: the number of parts (dividing the stage count) that
 // brings the grid closest to the SM count without exceeding it much.
-int choose_ksplit(int tiles, int kblocks, int n_sm) {
+int choose_ksplit(int tiles, int kblocks, int n_sm, int cap = 0) {
   int best = 1;
-  for (int s = 1; s <= kblocks && s <= 64; ++s) {
+  const int smax = cap > 0 ? std::min(cap, 64) : 64;
+  for (int s = 1; s <= kblocks && s <= smax; ++s) {
     if (kblocks % s) continue;
     if ((long long)tiles * s <= n_sm) best = s;
   }
@@ -628,7 +629,7 @@ int split_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
     gemm_step_inc(a.ctr, s);
     return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
   };
-  const int r = run_steps(a.nt, st, a.cap, one_step);
+  const int r = run_steps(a.nt, st, a.cap, one_step, a.graph_steps);
   if (r != LGB_OK) return r;
   if (a.nt == 0 && a.rho_out != nullptr)
     cudaMemcpyAsync(a.rho_out, a.rho0, NN * sizeof(double2), cudaMemcpyDeviceToDevice, st);
@@ -704,11 +705,13 @@ int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_s
   return e == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
-void split_set_ksplit(GemmSplit& sp, int Kd, int cta_budget) {
+void split_set_ksplit(GemmSplit& sp, int Kd, int cta_budget, int cap) {
+  // (a cap only lowers the factors, so the partial-tile buffers sized for the
+  // largest budget stay large enough)
   const int KT = kRowBytes / (sp.bf16 ? 2 : 4);
   const int t2 = (sp.NP / 128) * (sp.NP / 64);
-  sp.ks2 = choose_ksplit(t2, (int)(sp.Wp / KT), cta_budget);
-  sp.ks1 = Kd > 0 ? choose_ksplit(t2 * Kd, sp.NP / KT, cta_budget) : 1;
+  sp.ks2 = choose_ksplit(t2, (int)(sp.Wp / KT), cta_budget, cap);
+  sp.ks1 = Kd > 0 ? choose_ksplit(t2 * Kd, sp.NP / KT, cta_budget, cap) : 1;
 }
 
 size_t split_tpart_elems(int NP, int Kd, int n_sm, bool bf16) {

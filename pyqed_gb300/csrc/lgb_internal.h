@@ -160,6 +160,7 @@ struct GemmRunArgs {
   double2* obs_out = nullptr;      // this instance's rows
   double2* rho_out = nullptr;
   double2* states_out = nullptr;
+  int graph_steps = 16;            // RK4 steps per captured CUDA graph
   double check_tol = 0.0;          // per-step check (0: off)
   double* chk = nullptr;           // this instance's [2] check maxima
   double* chk_ws = nullptr;        // this instance's [8] check scratch
@@ -178,7 +179,7 @@ void gemm_step_inc(int* ctr, cudaStream_t st);
 // nt RK4 steps: eagerly, or as CUDA graphs of up to 16 steps captured once on
 // `cap` and replayed on `st` (one_step launches one step on the stream given)
 template <typename F>
-int run_steps(int nt, cudaStream_t st, cudaStream_t cap, F&& one_step);
+int run_steps(int nt, cudaStream_t st, cudaStream_t cap, F&& one_step, int graph_steps = 16);
 // split-precision schedule (lgb_gemm_tc.cu)
 int split_padded_dim(int N);
 size_t split_partial_slots(int N);
@@ -186,7 +187,7 @@ size_t split_tpart_elems(int NP, int Kd, int n_sm, bool bf16);
 size_t split_rpart_elems(int NP, int Kd, int n_sm, bool bf16);
 int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_sm, cudaStream_t st);
 // split-K factors of one instance for a CTA budget (SM count x waves)
-void split_set_ksplit(GemmSplit& sp, int Kd, int cta_budget);
+void split_set_ksplit(GemmSplit& sp, int Kd, int cta_budget, int cap = 0);
 int split_propagate(const GemmRunArgs& a, cudaStream_t st);
 
 }  // namespace lgb
@@ -209,6 +210,8 @@ struct lgb_plan {
   int opt_waves = 1;                       // LGB_OPT_GEMM_WAVES
   int opt_stall = 0;                       // LGB_OPT_TEST_STALL
   int opt_check = 0;                       // LGB_OPT_CHECK: 0 off, v: tolerance 10^-v
+  int opt_kcap = 0;                        // LGB_OPT_GEMM_KSPLIT: split-K cap (0: none)
+  int opt_gsteps = 16;                     // LGB_OPT_GRAPH_STEPS: RK4 steps per CUDA graph
   cudaStream_t cap_stream = nullptr;       // GEMM schedule: CUDA-graph capture
   int* d_ctr = nullptr;                    // GEMM schedule: device step counter
   void* blas_ws = nullptr;                 // cuBLAS workspace (graph capture allocates nothing)
@@ -269,8 +272,9 @@ struct lgb_plan {
 // ---- CUDA-graph step runner of the GEMM schedule (header-defined template) -------
 namespace lgb {
 template <typename F>
-int run_steps(int nt, cudaStream_t st, cudaStream_t cap, F&& one_step) {
-  constexpr int kGraphSteps = 16, kGraphMin = 32;
+int run_steps(int nt, cudaStream_t st, cudaStream_t cap, F&& one_step, int graph_steps) {
+  const int kGraphSteps = graph_steps > 0 ? graph_steps : 16;
+  const int kGraphMin = 2 * kGraphSteps;
   if (cap == nullptr || nt < kGraphMin) {
     for (int s = 0; s < nt; ++s) {
       const int r = one_step(st);

@@ -36,6 +36,17 @@ def test_candidates():
     assert all("tc_pairs" not in x["options"] for x in c)
 
 
+def test_gemm_candidates_cover_graph_length_and_split_k():
+    c = autotune.candidates([256], "3xtf32", "dense", 4)
+    gemm = [x["options"] for x in c if x["schedule"] == "gemm"]
+    assert {} in gemm and {"graph_steps": 32} in gemm
+    assert {"gemm_waves": 2} in gemm and {"gemm_ksplit": 4} in gemm
+    assert {"graph_steps": 32, "gemm_ksplit": 8} in gemm
+    # the plain precisions have no split-K shape to tune
+    c = autotune.candidates([256], "fp32", "dense", 4)
+    assert all(set(x["options"]) <= {"graph_steps"} for x in c)
+
+
 def test_bf16_candidates_keep_the_fp32_diagonal():
     # 3xBF16 on instances that fit the tensor-core kernel: only that kernel
     # (its diagonal of A is applied in FP32), never the GEMM schedule
@@ -60,10 +71,11 @@ def test_tune_selects_fastest_and_caches(tmp_path, monkeypatch):
 
     def timer(c):
         calls.append(c)
-        return fake[(c["schedule"], tuple(sorted(c["options"].items())))]
+        return fake.get((c["schedule"], tuple(sorted(c["options"].items()))), 7.0)
     r = autotune.tune(bi, dt=0.01, precision="3xtf32", timer=timer)
     assert (r["schedule"], r["options"], r["cached"]) == ("auto", {"tc_pairs": 0}, False)
-    assert len(r["timings_ms"]) == 3  # the invalid candidate (None) is dropped
+    n_cand = len(autotune.candidates(bi.dims, "3xtf32", bi.cops_kind, bi.n_cops))
+    assert len(r["timings_ms"]) == n_cand - 1  # the invalid candidate (None) is dropped
     n = len(calls)
     r2 = autotune.tune(bi, dt=0.01, precision="3xtf32", timer=timer)
     assert r2["cached"] and r2["options"] == {"tc_pairs": 0} and len(calls) == n

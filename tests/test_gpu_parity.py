@@ -419,6 +419,41 @@ def test_gemm_schedule_driven_vs_oracle(prec, tol):
         assert np.abs(res["observables"][b, :, 0] - obs[:, 0]).max() < tol * 10
 
 
+def test_gemm_tuning_options_change_only_the_schedule():
+    """The GEMM schedule's tuning options (steps per captured CUDA graph, the
+    split-K cap and waves) reschedule the same arithmetic: the results agree
+    with the default schedule within the precision's tolerance and with the
+    oracle."""
+    from pyqed_gb300.batch import prepare_batch
+    from pyqed_gb300.engine import Propagator
+    rng = np.random.default_rng(35)
+    N, nt, dt = 130, 40, 0.01
+    H, cops, rho0, O_ = _random_instance(rng, N, 3)
+    bi = prepare_batch([H], [cops], [rho0], [[O_]])
+    _, states = O.lindblad(H, rho0, cops, [O_], Nt=nt, dt=dt)
+    for prec, tol in (("fp32", TOL32), ("3xtf32", TOL32)):
+        out = {}
+        for opts in ({}, {"graph_steps": 8}, {"gemm_ksplit": 4}, {"gemm_ksplit": 1, "gemm_waves": 2},
+                     {"graph_steps": 32, "gemm_ksplit": 8}):
+            if prec == "fp32" and set(opts) - {"graph_steps"}:
+                continue
+            prop = Propagator(bi.dims, nt=nt, dt=dt, n_cops=bi.n_cops, cops_kind=bi.cops_kind, n_eops=1,
+                              precision=prec, schedule="gemm")
+            try:
+                for k, v in opts.items():
+                    prop.set_option(k, v)
+                prop.set_operators(bi.H, bi.cops, bi.eops, bi.dops)
+                o = prop.alloc_outputs(want_obs=True, want_rho=True)
+                prop.propagate_device(prop.to_device(bi.rho0), None, o)
+                prop.check_errors()
+                out[tuple(sorted(opts.items()))] = prop.unpack_rho(o[1])[0]
+            finally:
+                prop.close()
+        for k, r in out.items():
+            assert np.abs(r - states[-1]).max() < tol, (prec, k)
+            assert np.abs(r - out[()]).max() < tol, (prec, k)
+
+
 @pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32), ("3xtf32", TOL32)])
 def test_gemm_schedule_graph_replay_vs_oracle(prec, tol):
     """45 steps: two replays of a captured 16-step CUDA graph and one of a
