@@ -349,14 +349,15 @@ def run_gpu(args, ctx=None):
         traffic = None
         if args.workload == "exciton4096":
             # DRAM bytes per launch: operator/rho0 reads measured by ncu on a
-            # 304-instance case (3xTF32 23.1 MB, 3xBF16 23.3 MB, against 24.3 MB
-            # algorithmic) scaled by the algorithmic read bytes, plus the
+            # small case (3xTF32: 304 mixed instances, 23.1 MB against 24.3 MB
+            # algorithmic; 3xBF16: 152 instances of N = 64, 25.53 MB against
+            # 25.37 MB) scaled by the algorithmic read bytes, plus the
             # algorithmic writes (C(t), rho)
             d64 = bi.dims.astype(np.int64)
             npd = np.where(d64 <= 64, (d64 + 15) // 16 * 16, (d64 + 3) // 4 * 4)
             reads = int((npd * (npd + 2) * 8 * (2 + bi.n_eops)).sum() + (d64 ** 2 * 16).sum())
             writes = int(n_inst * nt * bi.n_eops * 16 + (d64 ** 2 * 16).sum())
-            traffic = int(reads * ((23.10 if chosen == "3xtf32" else 23.30) / 24.30)) + writes
+            traffic = int(reads * ((23.10 / 24.30) if chosen == "3xtf32" else (25.53 / 25.37))) + writes
         line["roofline"] = dict(bound="tensor", achieved=achieved, peak=pk, unit="TFLOP/s",
                                 frac=achieved / pk, traffic=traffic,
                                 # the split product runs three MMA products per algorithmic one
