@@ -471,19 +471,30 @@ def measure_adjoint(args, dev):
 # GEMMs against the plain FP32 GEMMs
 # ---------------------------------------------------------------------------
 def measure_large_n(args, dev):
-    """GUE N=256 (K=4, dt=0.01) and N=1024 (K=8, scale 0.02, rank-4 rho0,
-    dt=0.005): ms per RK4 step of each path over ``--large-nt`` steps, and the
-    max-abs rho error after 10 steps against the FP64 GPU check path (itself
-    within 1e-12 of the reference's complex128 result on the fixtures)."""
+    """GUE N=256 (K=4, dt=0.01, 10000 steps) and N=1024 (K=8, scale 0.02,
+    rank-4 rho0, dt=0.005, 1000 steps): ms per RK4 step of each path over
+    ``--large-nt`` steps, and each path's max-abs rho error after the
+    workload's full length against the reference's own ``_fast_lindblad``
+    result (tests/golden/gue256_long.npz: the whole final state;
+    gue1024_long.npz: rows 0..15 and the diagonal), when the fixture is
+    present and the seeded inputs match it."""
+    import hashlib
     import torch
     from pyqed_gb300 import workloads as W
     from pyqed_gb300.engine import Propagator, pack
     out = {}
+    gold = os.path.join(ROOT, "tests", "golden")
+
+    def digest(*arrays):
+        h = hashlib.sha256()
+        for a in arrays:
+            h.update(np.ascontiguousarray(a, dtype=np.complex128).tobytes())
+        return h.hexdigest()
     cases = [("gue256", dict(N=256, K=4, seed=2, dt=0.01, nt=10000)),
              ("gue1024", dict(N=1024, K=8, scale=0.02, rank=4, seed=4, dt=0.005, nt=1000))]
     for name, kw in cases:
         w = W.gue_instance(**kw)
-        N, K, dt = kw["N"], kw["K"], kw["dt"]
+        N, K, dt, nt_full = kw["N"], kw["K"], kw["dt"], kw["nt"]
         H, C, R0 = pack([w["H"]]), pack(w["c_ops"]), pack([w["rho0"]])
 
         def run(prec, nt, timed):
@@ -509,18 +520,28 @@ def measure_large_n(args, dev):
             rho = prop.unpack_rho(o[1])[0]
             prop.close()
             return ms, rho
-        _, ref = run("fp64", 10, False)
+        ref = None
+        fx = os.path.join(gold, name + "_long.npz")
+        if os.path.exists(fx):
+            g = np.load(fx)
+            if name == "gue256" and digest(w["H"], *w["c_ops"], w["rho0"]) == str(g["digest"]):
+                ref = lambda r, g=g: float(np.abs(r - g["rho"]).max())  # noqa: E731
+            elif name == "gue1024" and digest(w["H"], *w["c_ops"]) == str(g["digest_ops"]):
+                ref = lambda r, g=g: float(max(np.abs(r[:16, :] - g["rows"]).max(),  # noqa: E731
+                                               np.abs(np.diag(r) - g["diag"]).max()))
         flops = 64 * (1 + K) * N ** 3
         res = {}
         for prec in ("3xtf32", "3xbf16", "fp32"):
             ms, _ = run(prec, args.large_nt, True)
-            _, r10 = run(prec, 10, False)
-            res[prec] = dict(ms_per_step=ms, tflops_algorithmic=flops / (ms / 1e3) / 1e12,
-                             max_abs_err_rho_10_steps=float(np.abs(r10 - ref).max()))
+            res[prec] = dict(ms_per_step=ms, tflops_algorithmic=flops / (ms / 1e3) / 1e12)
+            if ref is not None:
+                _, rfull = run(prec, nt_full, False)
+                res[prec]["max_abs_err_rho_full_length"] = ref(rfull)
         for prec in ("3xtf32", "3xbf16"):
             res[prec]["speedup_over_fp32"] = res["fp32"]["ms_per_step"] / res[prec]["ms_per_step"]
-        out[name] = dict(N=N, K=K, dt=dt, steps_timed=args.large_nt, paths=res,
-                         reference="FP64 GPU GEMM schedule, 10 steps")
+        out[name] = dict(N=N, K=K, dt=dt, steps_timed=args.large_nt, steps_full=nt_full, paths=res,
+                         reference=("the reference's _fast_lindblad after %d steps (%s_long.npz)" % (nt_full, name)
+                                    if ref is not None else "fixture absent: errors not measured"))
     out["note"] = ("split paths: hand-written TMA + tcgen05 complex GEMMs (lgb_gemm_tc.cu); "
                    "fp32: cuBLAS CGEMM, pedantic math; algorithmic 64(1+K)N^3 flops per step")
     return out
