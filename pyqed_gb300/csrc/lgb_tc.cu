@@ -678,13 +678,18 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
   };
 
   // Bounded wait for the last commit; on time-out mark the instance and stop.
+  // What follows a time-out is best effort: MMAs possibly still in flight get
+  // one more bounded wait, and then the CTA goes on to free its tensor memory
+  // whether or not they drained -- a CTA that exited still holding it would
+  // make every later allocation on this SM wait forever, which is worse than
+  // a stalled pipe writing into columns nobody reads any more.
   const long long spin = p.spin > 0 ? p.spin : kSpinLimit;
   auto wait_mma = [&]() -> bool {
     const bool ok = mbar_wait(mbar, phase, spin);
     phase ^= 1u;
     if (gor<GR>(grp, !ok)) {
       if (tid == 0) p.err[b] = 5;  // LGB_ERR_TIMEOUT
-      mbar_wait(mbar, phase ^ 1u, spin);  // MMAs still in flight finish before TMEM is freed
+      mbar_wait(mbar, phase ^ 1u, spin);  // let MMAs still in flight finish (bounded)
       alive = false;
       return false;
     }
