@@ -1039,14 +1039,23 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
           u3 = c == 0 ? ci.y : -ci.x;
           brow = bd->bx[bcur][1];
         }
+        // the accumulator columns of group g + 1 are loaded while group g is
+        // processed (one tcgen05.wait::ld per group, after the group's work)
+        float pa1[2][4], pa0[2][4];
+        tmem_ld4(tlane + (uint32_t)ncol(1, j0), pa1[0]);
+        tmem_ld4(tlane + (uint32_t)ncol(0, j0), pa0[0]);
+        tmem_wait_ld();
 #pragma unroll
         for (int g = 0; g < NG; ++g) {
           const int col = j0 + g * 4;
-          float a1[4], a0[4], xo[4];
-          tmem_ld4(tlane + (uint32_t)ncol(1, col), a1);
-          tmem_ld4(tlane + (uint32_t)ncol(0, col), a0);
+          float xo[4];
+          const float* a1 = pa1[g & 1];
+          const float* a0 = pa0[g & 1];
+          if (g + 1 < NG) {
+            tmem_ld4(tlane + (uint32_t)ncol(1, col + 4), pa1[(g + 1) & 1]);
+            tmem_ld4(tlane + (uint32_t)ncol(0, col + 4), pa0[(g + 1) & 1]);
+          }
           if constexpr (MODE == 2) read_group(g, xo);
-          tmem_wait_ld();
           float q1x[4];
 #pragma unroll
           for (int e = 0; e < 4; ++e) q1x[e] = __shfl_xor_sync(0xffffffffu, a1[e], 16);
@@ -1108,6 +1117,7 @@ __device__ void tc_instance(const CtaParams& p, const int b, unsigned char* smem
           const float x4[4] = {xn2[0].x, xn2[0].y, xn2[1].x, xn2[1].y};
           write_group(g, x4);
           if (STAGE < 3 || p.n_drive == 0) inject(g, x4, ai_row);
+          if (g + 1 < NG) tmem_wait_ld();
         }
         tmem_wait_st();
         if constexpr (BD) {
