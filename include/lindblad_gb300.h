@@ -174,8 +174,10 @@ int lgb_plan_adjoint(lgb_plan_t plan, const double* rho0, const double* drive,
                      double* drho0_out, void* stream);
 
 /* Plan introspection: the schedule and precision in use, the bytes of
- * device workspace, the dynamic shared memory per CTA and the number of
- * kernel launches one propagate issues. */
+ * device workspace, the dynamic shared memory per CTA, the number of
+ * kernel launches one propagate issues and the number of instances that a
+ * propagate without the per-step check runs on the persistent split-precision
+ * kernel (LGB_OPT_GEMM_PERSIST). */
 typedef struct {
   int32_t schedule;
   int32_t precision;
@@ -183,6 +185,8 @@ typedef struct {
   int32_t launches_per_propagate;
   int64_t workspace_bytes;
   int64_t flops_per_step;   /* algorithmic real flops of one RK4 step, whole batch */
+  int32_t persistent_instances;
+  int32_t reserved;
 } lgb_plan_info_t;
 
 int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
@@ -204,6 +208,12 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
  *   LGB_OPT_GRAPH_STEPS GEMM schedule: RK4 steps captured per CUDA graph
  *                      (1..64, default 16; propagations of fewer than two
  *                      graphs' worth of steps launch directly)
+ *   LGB_OPT_GEMM_PERSIST split-precision GEMM schedule: 1 (default) runs a
+ *                      static instance with 64 < N <= 256 as one persistent
+ *                      launch (clusters of 8 CTAs, two grid barriers per RK4
+ *                      stage) when the device holds all its CTAs at once and
+ *                      the per-step check is off; 0 always uses the graph-
+ *                      replayed kernels
  *   LGB_OPT_CHECK      per-step check of the state, accumulated in FP64:
  *                      0 (default) off; v = 1..15 checks after every step
  *                      that |Tr rho(t) - Tr rho0| <= 10^-v and, for
@@ -223,7 +233,8 @@ typedef enum {
   LGB_OPT_TEST_STALL = 3,
   LGB_OPT_CHECK = 4,
   LGB_OPT_GEMM_KSPLIT = 5,
-  LGB_OPT_GRAPH_STEPS = 6
+  LGB_OPT_GRAPH_STEPS = 6,
+  LGB_OPT_GEMM_PERSIST = 7
 } lgb_option_t;
 
 int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value);

@@ -50,7 +50,7 @@ EXPORTS = [
 ]
 # tuning options (lgb_option_t)
 OPT = {"tc_pairs": 1, "gemm_waves": 2, "test_stall": 3, "check": 4, "gemm_ksplit": 5,
-       "graph_steps": 6}
+       "graph_steps": 6, "gemm_persist": 7}
 FLAG_ADJOINT = 1
 HEOM_DOUBLE_FIRST = 1
 HEOM_DIAG_SZ = 2
@@ -79,6 +79,7 @@ class PlanInfo(ctypes.Structure):
         ("schedule", ctypes.c_int32), ("precision", ctypes.c_int32),
         ("smem_bytes", ctypes.c_int32), ("launches_per_propagate", ctypes.c_int32),
         ("workspace_bytes", ctypes.c_int64), ("flops_per_step", ctypes.c_int64),
+        ("persistent_instances", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
 
 

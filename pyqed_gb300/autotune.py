@@ -64,9 +64,16 @@ def candidates(dims, precision, cops_kind, n_cops, n_drive=0):
         return out
     if dims.size <= _GEMM_MAX_INST:
         # the GEMM schedule: steps per captured CUDA graph, and for the split
-        # precisions the split-K shape (waves of CTAs, a cap on the factor)
+        # precisions the split-K shape (waves of CTAs, a cap on the factor).
+        # Split-precision static instances with 64 < N <= 256 run on the
+        # persistent kernel by default, which these options do not shape: the
+        # graph-replayed variants are timed with it switched off.
+        persist = split and n_drive == 0 and bool(np.any((dims > 64) & (dims <= 256)))
+        off = {"gemm_persist": 0} if persist else {}
+        if persist:
+            out.append(dict(schedule="gemm", options={}))
         for gs in (16, 32):
-            base = {} if gs == 16 else {"graph_steps": gs}
+            base = dict(off) if gs == 16 else dict(off, graph_steps=gs)
             out.append(dict(schedule="gemm", options=dict(base)))
             if split:
                 out.append(dict(schedule="gemm", options=dict(base, gemm_waves=2)))

@@ -336,10 +336,16 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
         q.NP = lgb::split_padded_dim(pl->dims[b]);
         q.Wp = (long long)(Kd + 2) * q.NP;
         q.bf16 = bf16;
+        // (a second copy of Ls and Rs for the persistent kernel where it may apply)
+        q.copies = q.NP <= 256 ? 2 : 1;
         for (int l = 0; l < 2; ++l) {
-          s = s ? s : dalloc(pl, &q.Ls[l], (size_t)2 * q.NP * q.Wp * ses);
-          s = s ? s : dalloc(pl, &q.Rs[l], (size_t)2 * q.NP * q.Wp * ses);
+          s = s ? s : dalloc(pl, &q.Ls[l], (size_t)q.copies * 2 * q.NP * q.Wp * ses);
+          s = s ? s : dalloc(pl, &q.Rs[l], (size_t)q.copies * 2 * q.NP * q.Wp * ses);
           s = s ? s : dalloc(pl, &q.Lks[l], (size_t)Kd * 2 * q.NP * q.NP * ses);
+        }
+        if (q.copies == 2) {
+          s = s ? s : dalloc(pl, &q.bar, sizeof(unsigned));
+          s = s ? s : dalloc(pl, &q.part, (size_t)lgb::persist_part_elems(q.NP) * sizeof(double2));
         }
         s = s ? s : dalloc(pl, &q.Tpart, Kd ? lgb::split_tpart_elems(q.NP, Kd, 2 * pl->n_sm, bf16) * sizeof(float2) : 0);
         s = s ? s : dalloc(pl, &q.Rpart, lgb::split_rpart_elems(q.NP, Kd, 2 * pl->n_sm, bf16) * sizeof(float2));
@@ -527,6 +533,7 @@ int lgb_plan_propagate(lgb_plan_t plan, const double* rho0, const double* drive_
       a.rho_out = p.rho_out ? p.rho_out + plan->off[b] : nullptr;
       a.states_out = p.states_out ? p.states_out + plan->soff[b] : nullptr;
       a.graph_steps = plan->opt_gsteps;
+      a.persist = plan->opt_persist != 0;
       a.check_tol = p.check_tol;
       a.chk = plan->d_chk + 2 * b;
       a.chk_ws = plan->d_chkws + 8 * b;
@@ -730,6 +737,10 @@ int lgb_plan_set_option(lgb_plan_t plan, int32_t option, int32_t value) {
       if (value != 0 && value != 1) return LGB_ERR_INVALID_ARG;
       plan->opt_stall = value;
       return LGB_OK;
+    case LGB_OPT_GEMM_PERSIST:
+      if (value != 0 && value != 1) return LGB_ERR_INVALID_ARG;
+      plan->opt_persist = value;
+      return LGB_OK;
     default:
       return LGB_ERR_INVALID_ARG;
   }
@@ -743,6 +754,8 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
                               plan->tcb_order.empty() ? plan->tc_smem : std::max(plan->tc_smem, plan->tcb_smem));
   info->launches_per_propagate = (plan->order.empty() ? 0 : 1) + (plan->order_w.empty() ? 0 : 1) +
                                  (plan->tc_order.empty() ? 0 : 1) + (plan->tcb_order.empty() ? 0 : 1);
+  info->persistent_instances = 0;
+  info->reserved = 0;
   if (plan->schedule == LGB_SCHED_GEMM) {
     // per instance: init (+ t0 observables) + per step (drive) + 4 x (G1, G2, epilogue);
     // split precision: init also converts X (2 kernels), the drive step also
@@ -754,7 +767,12 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info) {
     const int per_drive = pr.n_drive > 0 ? (split ? 3 : 1) : 0;
     const int init = 1 + (split ? 2 : 0) + (pr.obs_t0 && pr.n_eops ? 1 : 0);
     // (+1 per step: the step-counter increment; steps run as CUDA-graph replays when nt >= 32)
-    info->launches_per_propagate = pr.n_inst * (init + pr.nt * (4 * per_stage + per_drive + 1));
+    int n_ps = 0;
+    if (split && plan->opt_persist && pr.n_drive == 0 && pr.nt > 0)
+      for (const auto& q : plan->gsplit) n_ps += q.persist ? 1 : 0;
+    info->persistent_instances = n_ps;
+    info->launches_per_propagate =
+        (pr.n_inst - n_ps) * (init + pr.nt * (4 * per_stage + per_drive + 1)) + n_ps * (init + 1);
   }
   info->workspace_bytes = (int64_t)plan->ws_bytes;
   info->flops_per_step = plan->flops_per_step;

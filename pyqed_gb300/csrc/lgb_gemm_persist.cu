@@ -1,0 +1,613 @@
+// Persistent split-precision (3xTF32 / 3xBF16) schedule for one instance of
+// 64 < N <= 256 (padded NP = 128 or 256): the whole propagation in one launch.
+//
+// The graph-replayed schedule (lgb_gemm_tc.cu) spends a launch per GEMM,
+// split-K sum and epilogue, 17 per RK4 step; at NP = 256 those dependent
+// launches, not the tensor pipe, set its speed.  Here the same products of
+// pyqed/oqs.py:697-715,
+//     G1  T_k = L_k X,      G2  R = [A | X | T_1..T_K] . [X ; A^dag ; L_1^dag ; ..],
+// and the RK4 combination of pyqed/phys.py:1051-1064 run as two phases per
+// stage separated by grid-wide barriers (8 per step):
+//
+// * The grid is one cluster of 4 CTAs per 64 x 32 complex tile of R
+//   ((NP/64)(NP/32) clusters, 128 CTAs at NP = 256, one CTA per SM; clusters
+//   of 4 because a GB300 holds 15 clusters of 8 such CTAs, 36 of 4).  Every
+//   work item is an M = 128, N = 64 tcgen05 product (64 x 32 complex, the
+//   interleaved real form of lgb_tc.cu) over a K range, fed by a 3-stage TMA
+//   ring of 128-byte-swizzled rows (thread 0) and issued by one thread
+//   (thread 32) as the three leading split products hi*hi, hi*lo, lo*hi.
+// * G2: the 4 CTAs of a cluster split its tile's K extent (K + 2) NP four
+//   ways; G1: they take the K products of the tile position, each split
+//   s1 = 4 / K ways (rounded down to a power of two).  The split partials
+//   are summed through distributed shared memory: every CTA stores its
+//   combined rows (FP32) into the receive buffer of the CTA that owns them,
+//   one hardware cluster barrier, and the owner adds the sources in a fixed
+//   order (deterministic; no partial tiles in global memory, no extra phase).
+// * The owner of rows [16r, 16r + 16) of the G2 tile keeps rho, the RK4 sum,
+//   the Kahan compensation and the stage input of its 512 elements in
+//   registers for the whole run; it applies the stage combination, writes
+//   the next stage input into both split operand layouts and, after stage 3,
+//   the observables' partials, the stored states and the final rho.
+// * The operand arrays hold two copies (rows [0, 2NP) and [2NP, 4NP)); stage
+//   s reads copy s % 2 and writes the next X into the other copy, so no CTA
+//   overwrites an operand that another CTA may still be loading.
+//
+// Every mbarrier wait and every grid-barrier wait is bounded (a grid barrier
+// gives up after 1 s of global-timer time).  A wait that runs out sets
+// LGB_ERR_TIMEOUT; from the next grid barrier on the CTA skips all work but
+// still takes part in every cluster barrier, so that the hardware cluster
+// barriers always complete and the kernel ends.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "lgb_common.cuh"
+#include "lgb_internal.h"
+#include "lgb_split.cuh"
+#include "lgb_umma.cuh"
+
+namespace lgb {
+
+namespace {
+
+using namespace umma;
+using namespace splitk;
+
+constexpr int kPsThreads = 128;
+constexpr int kPsCluster = 4;
+constexpr int kPsCols = kPersistQRows / 2;               // complex columns of a tile (64 rows)
+constexpr int kPsOwn = 64 / kPsCluster;                  // G2 tile rows owned by one CTA
+constexpr int kPsStages = 3;
+constexpr int kPsRowBytes = kPersistRowBytes;            // K bytes per operand row and ring stage
+constexpr uint32_t kPsTileP = 128 * kPsRowBytes;         // 16 KB: one level of the M-side operand
+constexpr uint32_t kPsTileQ = 2 * kPsCols * kPsRowBytes; // 8 KB: one level of the N-side operand
+constexpr uint32_t kPsStageBytes = 2 * kPsTileP + 2 * kPsTileQ;  // P hi, P lo, Q hi, Q lo
+constexpr uint32_t kPsRing = kPsStages * kPsStageBytes;  // 144 KB
+constexpr uint32_t kPsRecv = 64 * 2 * kPsCols * 4;       // 16 KB: tile rows x parts x columns, FP32
+constexpr uint32_t kPsXs = kPsOwn * kPsCols * sizeof(float2);  // 4 KB: the owner's next X rows
+constexpr uint32_t kPsSmem = kPsRing + 2 * kPsRecv + kPsXs + 1024;  // + alignment slack
+constexpr unsigned long long kPsBarNs = 1000000000ull;   // grid-barrier wait bound (1 s)
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_idx() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+// shared::cta address of this CTA -> the same offset in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t mapa(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster4(uint32_t addr, float a, float b, float c, float d) {
+  asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c),
+               "f"(d)
+               : "memory");
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// order this thread's generic global writes before later async-proxy (TMA) reads
+__device__ __forceinline__ void fence_proxy_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+// hi and lo parts of 8 consecutive values -> 16-byte-aligned vector stores
+template <bool BF16>
+__device__ __forceinline__ void store8_split(typename SElem<BF16>::T* hd, typename SElem<BF16>::T* ld,
+                                             const float* v) {
+  using T = typename SElem<BF16>::T;
+  constexpr int W = 8 * (int)sizeof(T) / 4;  // 32-bit words per part
+  uint32_t hw[W], lw[W];
+  if constexpr (BF16) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      T h0, l0, h1, l1;
+      SElem<true>::split(v[2 * k], h0, l0);
+      SElem<true>::split(v[2 * k + 1], h1, l1);
+      hw[k] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+      lw[k] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float h, l;
+      SElem<false>::split(v[k], h, l);
+      hw[k] = __float_as_uint(h);
+      lw[k] = __float_as_uint(l);
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < W / 4; ++w) {
+    reinterpret_cast<uint4*>(hd)[w] = make_uint4(hw[4 * w], hw[4 * w + 1], hw[4 * w + 2], hw[4 * w + 3]);
+    reinterpret_cast<uint4*>(ld)[w] = make_uint4(lw[4 * w], lw[4 * w + 1], lw[4 * w + 2], lw[4 * w + 3]);
+  }
+}
+
+struct PsMaps {
+  CUtensorMap p1h, p1l;  // G1 M side: the L_k rows (K x 2NP rows, pitch NP)
+  CUtensorMap p2h, p2l;  // G2 M side: Ls, both copies (4NP rows, pitch Wp)
+  CUtensorMap qh, ql;    // N side of both: Rs, both copies (4NP rows, pitch Wp, 64-row boxes)
+};
+
+struct PsArgs {
+  int N = 0, NP = 0, K = 0, E = 0, nt = 0, diag = 0, obs_t0 = 0;
+  int s1 = 1, nkb1 = 0, nkb2 = 0, tn = 0;  // tn: column tiles (NP / 32)
+  long long Wp = 0;
+  double dt = 0.0;
+  void* Ls[2] = {nullptr, nullptr};
+  void* Rs[2] = {nullptr, nullptr};
+  float2* rho = nullptr;         // FP32 state (read at the start, written at the end)
+  const float2* Dm = nullptr;    // diagonal-collapse dissipator (diag)
+  const double2* Ot = nullptr;   // E x N x N observables transposed
+  double2* obs_out = nullptr;    // this instance's rows
+  double2* part = nullptr;       // [2][16][grid] observable partials
+  unsigned* bar = nullptr;       // grid-barrier counter, zero at launch
+  int* err = nullptr;
+  StepOut so;
+};
+
+template <bool BF16>
+__global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads, 1)
+    persist_rk4_kernel(const __grid_constant__ PsMaps m, const PsArgs a) {
+  using T = typename SElem<BF16>::T;
+  extern __shared__ unsigned char ps_smem[];
+  __shared__ uint64_t full[kPsStages], empty[kPsStages], done;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_dead;
+  __shared__ double s_red[4][16][2];
+  constexpr int KT = kPsRowBytes / (BF16 ? 2 : 4);  // K elements per ring stage
+  constexpr int KSTEPS = KT / (BF16 ? 16 : 8);      // MMA K-steps per ring stage (32 B each)
+  constexpr uint32_t id = idesc(BF16 ? kFmtBF16 : kFmtTF32, 128, 2 * kPsCols, false, false);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int rank = (int)cluster_rank();
+  const int cid = (int)cluster_idx();
+  const int I = cid / a.tn, J = cid % a.tn;  // the cluster's G2 tile
+  const int N = a.N, NP = a.NP;
+  const long long Wp = a.Wp;
+  const uint32_t sraw = smem_u32(ps_smem);
+  const uint32_t sb = (sraw + 1023u) & ~1023u;  // ring base (1 KB aligned for the swizzled tiles)
+  unsigned char* gb = ps_smem + (sb - sraw);
+  const uint32_t recv = sb + kPsRing;           // two receive buffers, kPsRecv apart
+  const float* recvf = reinterpret_cast<const float*>(gb + kPsRing);
+  float2* xs = reinterpret_cast<float2*>(gb + kPsRing + 2 * kPsRecv);
+
+  if (tid == 0) {
+    for (int s = 0; s < kPsStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    mbar_fence_init();
+    s_dead = *reinterpret_cast<volatile int*>(a.err) == 5;
+  }
+  if (warp == 0) {
+    tmem_alloc(&tmem_base, 2 * kPsCols);
+    tmem_relinquish();
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  cluster_sync_all();  // every CTA of the cluster runs before the first remote store
+  const uint32_t tmem = tmem_base;
+  bool dead = s_dead != 0;
+
+  // owned elements of the G2 tile: rows orow + (tid >> 5) + 4q, column tid & 31
+  const int orow = kPsOwn * rank, ocol = tid & 31;
+  float2 rr[4], ra[4], kc[4], xc[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = 64 * I + orow + (tid >> 5) + 4 * q, j = kPsCols * J + ocol;
+    rr[q] = (i < N && j < N) ? a.rho[(long long)i * N + j] : make_float2(0.f, 0.f);
+    ra[q] = kc[q] = make_float2(0.f, 0.f);
+    xc[q] = rr[q];
+  }
+  uint32_t kit = 0, nitem = 0, nred = 0, nbar = 0;
+
+  // One product over ring stages [kb0, kb1) into the TMEM accumulator.
+  auto item = [&](const CUtensorMap* ph, const CUtensorMap* pl, int prow, int qrow, int kb0, int kb1) {
+    if (tid == 0) {
+      fence_proxy_global();
+      bool ok = true;
+      for (int kb = kb0; kb < kb1; ++kb) {
+        const uint32_t it = kit + (uint32_t)(kb - kb0);
+        const int s = (int)(it % kPsStages);
+        if (!mbar_wait(&empty[s], ((it / kPsStages) & 1) ^ 1, kGemmSpin)) {
+          ok = false;
+          break;
+        }
+        mbar_expect_tx(&full[s], kPsStageBytes);
+        const uint32_t st = sb + s * kPsStageBytes;
+        const int x = kb * KT;
+        tma_load_2d(st, ph, x, prow, &full[s]);
+        tma_load_2d(st + kPsTileP, pl, x, prow, &full[s]);
+        tma_load_2d(st + 2 * kPsTileP, &m.qh, x, qrow, &full[s]);
+        tma_load_2d(st + 2 * kPsTileP + kPsTileQ, &m.ql, x, qrow, &full[s]);
+      }
+      if (!ok) atomicExch(a.err, 5);  // LGB_ERR_TIMEOUT
+    } else if (tid == 32) {
+      fence_after_sync();
+      bool ok = true;
+      for (int kb = kb0; kb < kb1; ++kb) {
+        const uint32_t it = kit + (uint32_t)(kb - kb0);
+        const int s = (int)(it % kPsStages);
+        if (!mbar_wait(&full[s], (it / kPsStages) & 1, kGemmSpin)) {
+          ok = false;
+          break;
+        }
+        fence_after_sync();
+        const uint32_t st = sb + s * kPsStageBytes;
+#pragma unroll
+        for (int ks = 0; ks < KSTEPS; ++ks) {
+          const uint64_t dph = sdesc_sw128(st + 32 * ks);
+          const uint64_t dpl = sdesc_sw128(st + kPsTileP + 32 * ks);
+          const uint64_t dqh = sdesc_sw128(st + 2 * kPsTileP + 32 * ks);
+          const uint64_t dql = sdesc_sw128(st + 2 * kPsTileP + kPsTileQ + 32 * ks);
+          mma_k<BF16>(tmem, dph, dqh, id, (kb > kb0 || ks > 0) ? 1u : 0u);
+          mma_k<BF16>(tmem, dph, dql, id, 1u);
+          mma_k<BF16>(tmem, dpl, dqh, id, 1u);
+        }
+        mma_commit(&empty[s]);  // ring stage s is free once these MMAs completed
+      }
+      mma_commit(&done);
+      if (!ok) atomicExch(a.err, 5);
+    }
+    __syncwarp();
+    kit += (uint32_t)(kb1 - kb0);
+  };
+
+  // Wait for the item's MMAs, combine the partner lanes and store this CTA's
+  // rows (split source `src`) into the receive buffers of their owners:
+  // tile row i belongs to CTA owner0 + i / rows_per.  A row's 8 four-float
+  // chunks are stored at chunk ^ (i % 8), which spreads one store
+  // instruction of a warp over the banks.
+  auto push = [&](int src, int rows_per, int owner0) {
+    const uint32_t buf = recv + (nred & 1) * kPsRecv;
+    if (!mbar_wait(&done, nitem & 1, kGemmSpin)) atomicExch(a.err, 5);
+    ++nitem;
+    fence_after_sync();
+    const int c = lane >> 4, i = warp * 16 + (lane & 15);
+    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+    const float sg = c == 0 ? -1.f : 1.f;
+    float v[kPsCols];
+#pragma unroll
+    for (int h = 0; h < kPsCols / 16; ++h) {
+      float p1[16], p0[16];
+      tmem_ld16(tl + 32 * h, p1);
+      tmem_ld16(tl + 32 * h + 16, p0);
+      tmem_wait_ld();
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const float x = __shfl_xor_sync(0xffffffffu, p1[e], 16);
+        v[16 * h + e] = fmaf(sg, x, p0[e]);
+      }
+    }
+    fence_before_sync();
+    const int ow = owner0 + i / rows_per, rl = i % rows_per, sw = i & 7;
+    const uint32_t dst = mapa(buf + (uint32_t)(((src * rows_per + rl) * 2 + c) * kPsCols * 4), (uint32_t)ow);
+#pragma unroll
+    for (int q = 0; q < kPsCols / 4; ++q)
+      st_cluster4(dst + 16u * (uint32_t)(q ^ sw), v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  };
+
+  auto gsync = [&]() {
+    fence_proxy_global();
+    __syncthreads();
+    ++nbar;
+    if (tid == 0) {
+      int d = s_dead;
+      if (!d) {
+        __threadfence();
+        red_release_add(a.bar, 1u);
+        const unsigned target = nbar * gridDim.x;
+        const unsigned long long t0 = gtimer();
+        while (ld_acquire(a.bar) < target) {
+          if (gtimer() - t0 > kPsBarNs) {
+            d = 1;
+            atomicExch(a.err, 5);
+            break;
+          }
+        }
+        __threadfence();
+        if (*reinterpret_cast<volatile int*>(a.err) == 5) d = 1;
+      }
+      s_dead = d;
+    }
+    __syncthreads();
+    dead = s_dead != 0;
+  };
+
+  T* const LH = reinterpret_cast<T*>(a.Ls[0]);
+  T* const LL = reinterpret_cast<T*>(a.Ls[1]);
+  T* const RH = reinterpret_cast<T*>(a.Rs[0]);
+  T* const RL = reinterpret_cast<T*>(a.Rs[1]);
+  const float sixth = (float)(a.dt / 6.0);
+
+  // tile row i, column col of an owner's receive buffer (rows_per rows per source)
+  auto roff = [](int src, int rows_per, int rl, int c, int i, int col) {
+    return ((src * rows_per + rl) * 2 + c) * kPsCols + 4 * ((col >> 2) ^ (i & 7)) + (col & 3);
+  };
+
+  for (int step = 0; step < a.nt; ++step) {
+    for (int stage = 0; stage < 4; ++stage) {
+      const int cp = stage & 1, nx = cp ^ 1;  // operand copy read / written by this stage
+      // ---- G1: T_k = L_k X, K products of the tile position split s1 ways ----------
+      if (a.K > 0) {
+        const int groups = kPsCluster / a.s1, g = rank / a.s1, zz = rank % a.s1;
+        const int rows_per = 64 / a.s1;
+        for (int k0 = 0; k0 < a.K; k0 += groups) {
+          const int k = k0 + g;
+          const bool act = k < a.K && !dead;
+          if (act) {
+            item(&m.p1h, &m.p1l, k * 2 * NP + 128 * I, cp * 2 * NP + 2 * kPsCols * J,
+                 zz * a.nkb1 / a.s1, (zz + 1) * a.nkb1 / a.s1);
+            push(zz, rows_per, g * a.s1);
+          }
+          cluster_sync_all();
+          const float* rb = recvf + (nred & 1) * (kPsRecv / 4);
+          ++nred;
+          if (act) {
+            // owned rows [zz rows_per, +rows_per) of T_k -> M-side block 2 + k of this
+            // copy, 8 columns of one row part per task
+            for (int q = 0; q < rows_per / 16; ++q) {
+              const int e = tid + 128 * q;
+              const int oct = e & 3, c = (e >> 2) & 1, rl = e >> 3;
+              const int i = zz * rows_per + rl;
+              float v[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) v[u] = 0.f;
+              for (int src = 0; src < a.s1; ++src) {
+                const float* b = rb + ((src * rows_per + rl) * 2 + c) * kPsCols;
+                const float4 lo4 = *reinterpret_cast<const float4*>(b + 4 * ((2 * oct) ^ (i & 7)));
+                const float4 hi4 = *reinterpret_cast<const float4*>(b + 4 * ((2 * oct + 1) ^ (i & 7)));
+                v[0] += lo4.x, v[1] += lo4.y, v[2] += lo4.z, v[3] += lo4.w;
+                v[4] += hi4.x, v[5] += hi4.y, v[6] += hi4.z, v[7] += hi4.w;
+              }
+              const long long row = (long long)cp * 2 * NP + mrow(c, 64 * I + i);
+              const long long colg = (long long)(2 + k) * NP + kPsCols * J + 8 * oct;
+              store8_split<BF16>(LH + row * Wp + colg, LL + row * Wp + colg, v);
+            }
+          }
+        }
+        gsync();
+      }
+      // ---- G2: R = Ls . Rs^T, the tile's K extent split over the cluster -----------
+      if (!dead) {
+        item(&m.p2h, &m.p2l, cp * 2 * NP + 128 * I, cp * 2 * NP + 2 * kPsCols * J,
+             rank * a.nkb2 / kPsCluster, (rank + 1) * a.nkb2 / kPsCluster);
+        push(rank, kPsOwn, 0);
+      }
+      cluster_sync_all();
+      const float* rb = recvf + (nred & 1) * (kPsRecv / 4);
+      ++nred;
+      bool fin = true;
+      if (!dead) {
+        const float cst = (float)((stage == 2) ? a.dt : 0.5 * a.dt);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int r = (tid >> 5) + 4 * q, i = orow + r;
+          float2 R = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int src = 0; src < kPsCluster; ++src) {
+            R.x += rb[roff(src, kPsOwn, r, 0, i, ocol)];
+            R.y += rb[roff(src, kPsOwn, r, 1, i, ocol)];
+          }
+          const int ig = 64 * I + i, jg = kPsCols * J + ocol;
+          const bool in = ig < N && jg < N;
+          if (a.diag && in) cmac(R, a.Dm[(long long)ig * N + jg], xc[q]);
+          float2 xn;
+          if (stage == 0) {
+            ra[q] = R;
+            xn = caxpy(rr[q], cst, R);
+          } else if (stage < 3) {
+            ra[q] = caxpy(ra[q], 2.f, R);
+            xn = caxpy(rr[q], cst, R);
+          } else {
+            // Kahan-compensated rho += dt/6 (k1 + 2 k2 + 2 k3 + k4)
+            const float yx = fmaf(sixth, ra[q].x + R.x, -kc[q].x), yy = fmaf(sixth, ra[q].y + R.y, -kc[q].y);
+            const float tx = rr[q].x + yx, ty = rr[q].y + yy;
+            kc[q] = make_float2((tx - rr[q].x) - yx, (ty - rr[q].y) - yy);
+            rr[q] = make_float2(tx, ty);
+            xn = rr[q];
+            fin = fin && isfinite(tx) && isfinite(ty);
+          }
+          if (!in) xn = make_float2(0.f, 0.f);
+          xc[q] = xn;
+          xs[r * kPsCols + ocol] = xn;
+        }
+      }
+      __syncthreads();
+      if (!dead) {
+        // N-side block 0 (X^T) of the next copy: row (p, j), 8 of the owner's 16 columns
+        {
+          const int p = (tid >> 5) & 1, col = tid & 31, half = tid >> 6;
+          const long long row = (long long)nx * 2 * NP + ncol(p, kPsCols * J + col);
+          const long long c0 = 64LL * I + orow + 8 * half;
+          float v[8];
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            const float2 x = xs[(8 * half + r) * kPsCols + col];
+            v[r] = p == 0 ? x.x : x.y;
+          }
+          store8_split<BF16>(RH + row * Wp + c0, RL + row * Wp + c0, v);
+        }
+        // M-side block 1 (X rows) of the next copy: row (c, i), 8 of the tile's 32 columns
+        {
+          const int oct = tid & 3, c = (tid >> 2) & 1, r = tid >> 3;
+          const long long row = (long long)nx * 2 * NP + mrow(c, 64 * I + orow + r);
+          const long long c0 = (long long)NP + kPsCols * J + 8 * oct;
+          float v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const float2 x = xs[r * kPsCols + 8 * oct + u];
+            v[u] = c == 0 ? x.x : x.y;
+          }
+          store8_split<BF16>(LH + row * Wp + c0, LL + row * Wp + c0, v);
+        }
+      }
+      if (stage == 3 && !dead) {
+        if (__syncthreads_or(!fin) && tid == 0) atomicCAS(a.err, 0, 4);  // LGB_ERR_NONFINITE
+        double2* state_out = a.so.state_at(step, (long long)N * N);
+        double2* rho_out = step == a.nt - 1 ? a.so.rho_out : nullptr;
+        if (state_out != nullptr || rho_out != nullptr) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int ig = 64 * I + orow + (tid >> 5) + 4 * q, jg = kPsCols * J + ocol;
+            if (ig < N && jg < N) {
+              const double2 rd = make_double2(rr[q].x, rr[q].y);
+              if (state_out != nullptr) state_out[(long long)ig * N + jg] = rd;
+              if (rho_out != nullptr) rho_out[(long long)ig * N + jg] = rd;
+            }
+          }
+        }
+        for (int e = 0; e < a.E; ++e) {
+          double sx = 0.0, sy = 0.0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int ig = 64 * I + orow + (tid >> 5) + 4 * q, jg = kPsCols * J + ocol;
+            if (ig < N && jg < N) {
+              const double2 o = a.Ot[(long long)e * N * N + (long long)ig * N + jg];
+              sx += o.x * rr[q].x - o.y * rr[q].y;
+              sy += o.x * rr[q].y + o.y * rr[q].x;
+            }
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
+          }
+          if (lane == 0) {
+            s_red[warp][e][0] = sx;
+            s_red[warp][e][1] = sy;
+          }
+        }
+        __syncthreads();
+        if (tid < a.E) {
+          const double sx = (s_red[0][tid][0] + s_red[1][tid][0]) + (s_red[2][tid][0] + s_red[3][tid][0]);
+          const double sy = (s_red[0][tid][1] + s_red[1][tid][1]) + (s_red[2][tid][1] + s_red[3][tid][1]);
+          a.part[((long long)(step & 1) * 16 + tid) * gridDim.x + blockIdx.x] = make_double2(sx, sy);
+        }
+      }
+      gsync();
+      if (stage == 3 && !dead && blockIdx.x == 0 && tid < a.E) {
+        // every CTA's partial of this step is in: fixed-order FP64 sum
+        const double2* pp = a.part + ((long long)(step & 1) * 16 + tid) * gridDim.x;
+        double sx = 0.0, sy = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) {
+          const volatile double* vp = reinterpret_cast<const volatile double*>(pp + b);
+          sx += vp[0];
+          sy += vp[1];
+        }
+        a.obs_out[((long long)step + a.obs_t0) * a.E + tid] = make_double2(sx, sy);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int ig = 64 * I + orow + (tid >> 5) + 4 * q, jg = kPsCols * J + ocol;
+    if (!dead && ig < N && jg < N) a.rho[(long long)ig * N + jg] = rr[q];
+  }
+  fence_before_sync();
+  __syncthreads();
+  cluster_sync_all();  // no CTA leaves while a peer may still address its shared memory
+  if (warp == 0) tmem_dealloc(tmem, 2 * kPsCols);
+}
+
+int grid_of(int NP) { return kPsCluster * (NP / 64) * (NP / kPsCols); }
+
+}  // namespace
+
+bool persist_supported(int NP, bool bf16) {
+  if (NP != 128 && NP != 256) return false;
+  const void* fn = bf16 ? reinterpret_cast<const void*>(&persist_rk4_kernel<true>)
+                        : reinterpret_cast<const void*>(&persist_rk4_kernel<false>);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPsSmem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid_of(NP));
+  cfg.blockDim = dim3(kPsThreads);
+  cfg.dynamicSmemBytes = kPsSmem;
+  int nc = 0;
+  if (cudaOccupancyMaxActiveClusters(&nc, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  // every cluster co-resident: the grid barriers need all CTAs running at once
+  return nc * kPsCluster >= grid_of(NP);
+}
+
+int persist_part_elems(int NP) { return 2 * 16 * grid_of(NP); }
+
+int persist_propagate(const GemmRunArgs& a, cudaStream_t st) {
+  const GemmSplit& sp = a.sp;
+  const int NP = sp.NP;
+  const int KT = kPsRowBytes / (sp.bf16 ? 2 : 4);
+  PsArgs p;
+  p.N = a.g.N;
+  p.NP = NP;
+  p.K = a.Kdense;
+  p.E = a.E;
+  p.nt = a.nt;
+  p.diag = a.diag;
+  p.obs_t0 = a.obs_t0;
+  p.nkb1 = NP / KT;
+  p.nkb2 = (int)(sp.Wp / KT);
+  int s1 = kPsCluster;
+  while (s1 > 1 && (a.Kdense * s1 > kPsCluster || s1 > p.nkb1)) s1 >>= 1;
+  p.s1 = s1;
+  p.tn = NP / kPsCols;
+  p.Wp = sp.Wp;
+  p.dt = a.dt;
+  for (int l = 0; l < 2; ++l) {
+    p.Ls[l] = sp.Ls[l];
+    p.Rs[l] = sp.Rs[l];
+  }
+  p.rho = reinterpret_cast<float2*>(a.g.rho);
+  p.Dm = reinterpret_cast<const float2*>(a.g.Dm);
+  p.Ot = a.g.Ot;
+  p.obs_out = a.obs_out;
+  p.part = sp.part;
+  p.bar = sp.bar;
+  p.err = a.g.err;
+  p.so.obs_t0 = a.obs_t0;
+  p.so.nt = a.nt;
+  p.so.store_every = a.store_every;
+  p.so.states_out = a.states_out;
+  p.so.rho_out = a.rho_out;
+  if (p.nkb2 < kPsCluster || (p.K > 0 && p.nkb1 < p.s1)) return LGB_ERR_UNSUPPORTED;
+  PsMaps mp;
+  mp.p1h = sp.map_ps[0];
+  mp.p1l = sp.map_ps[1];
+  mp.p2h = sp.map_ps[2];
+  mp.p2l = sp.map_ps[3];
+  mp.qh = sp.map_ps[4];
+  mp.ql = sp.map_ps[5];
+  if (cudaMemsetAsync(sp.bar, 0, sizeof(unsigned), st) != cudaSuccess) return LGB_ERR_CUDA;
+  const dim3 grid(grid_of(NP));
+  if (sp.bf16)
+    persist_rk4_kernel<true><<<grid, kPsThreads, kPsSmem, st>>>(mp, p);
+  else
+    persist_rk4_kernel<false><<<grid, kPsThreads, kPsSmem, st>>>(mp, p);
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
+}  // namespace lgb

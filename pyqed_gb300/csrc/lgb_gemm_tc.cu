@@ -35,6 +35,7 @@
 
 #include "lgb_common.cuh"
 #include "lgb_internal.h"
+#include "lgb_split.cuh"
 #include "lgb_umma.cuh"
 
 namespace lgb {
@@ -42,10 +43,10 @@ namespace lgb {
 namespace {
 
 using namespace umma;
+using namespace splitk;
 
 constexpr int kGThreads = 128;
 constexpr int kStages = 4;
-constexpr int kRowBytes = 64;              // K bytes per row and stage (one 64-byte swizzle atom)
 constexpr int kPRows = 128;                // M-side rows per tile (64 complex rows)
 constexpr int kQRows = 256;                // N-side rows per tile (128 complex columns)
 constexpr uint32_t kPBytes = kPRows * kRowBytes;  // one level of P per stage
@@ -53,45 +54,6 @@ constexpr uint32_t kQBytes = kQRows * kRowBytes;
 constexpr uint32_t kStageBytes = 2 * kPBytes + 2 * kQBytes;
 constexpr uint32_t kGemmSmem = kStages * kStageBytes;  // 192 KB
 constexpr int kStagePitch = 129;                       // float2 per staged output row
-// Poll bound of the pipeline waits: far above a tile's main loop (< 1 ms), far
-// below a stuck GPU.
-constexpr long long kGemmSpin = 1LL << 22;
-
-__device__ __forceinline__ int mrow(int c, int i) { return ((i >> 4) << 5) + (c << 4) + (i & 15); }
-__device__ __forceinline__ int ncol(int p, int j) { return ((j >> 4) << 5) + ((1 - p) << 4) + (j & 15); }
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
-                                            uint64_t* mbar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(mbar))
-      : "memory");
-}
-
-// K-major shared-memory descriptor with the 64-byte swizzle: rows 64 B apart,
-// 8-row groups SBO = 512 B apart, layout type 4 (bits 61-63), version 1.
-__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)1 << 16;            // leading byte offset (unused within one atom)
-  d |= (uint64_t)(512 >> 4) << 32;   // stride byte offset
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)4 << 61;
-  return d;
-}
-
-template <bool BF16>
-__device__ __forceinline__ void mma_k(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
-  if constexpr (BF16) {
-    mma_f16(d, a, b, id, acc);
-  } else {
-    mma_tf32(d, a, b, id, acc);
-  }
-}
 
 struct CgArgs {
   int p_row0 = 0, p_batch_rows = 0;  // M-side: first row of this product, rows per batch
@@ -227,26 +189,6 @@ __global__ void __launch_bounds__(kGThreads, 1)
 }
 
 // ---- split conversions ------------------------------------------------------------------
-template <bool BF16> struct SElem;
-template <> struct SElem<false> {
-  using T = float;
-  __device__ static void split(float x, T& h, T& l) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    const float hf = __uint_as_float(r);
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x - hf));
-    h = hf;
-    l = __uint_as_float(r);
-  }
-};
-template <> struct SElem<true> {
-  using T = __nv_bfloat16;
-  __device__ static void split(float x, T& h, T& l) {
-    h = __float2bfloat16_rn(x);
-    l = __float2bfloat16_rn(x - __bfloat162float(h));
-  }
-};
-
 // Row block: dst row mrow(c, i), column coff + j  <-  component c of src[i][j]
 // (batched: blockIdx.y = batch).
 template <bool BF16>
@@ -516,16 +458,19 @@ EncodeFn encode_fn() {
 
 // 2D map over a K-major split array (rows x pitch elements), box = 64 bytes x
 // box_rows, 64-byte swizzle.
-bool make_map(CUtensorMap* m, void* base, bool bf16, long long rows, long long pitch, int box_rows) {
+// (row_bytes 128: the 128-byte swizzle of the persistent kernel)
+bool make_map(CUtensorMap* m, void* base, bool bf16, long long rows, long long pitch, int box_rows,
+              int row_bytes = kRowBytes) {
   EncodeFn fn = encode_fn();
   if (fn == nullptr) return false;
   const int esz = bf16 ? 2 : 4;
   cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(pitch * esz)};
-  cuuint32_t box[2] = {(cuuint32_t)(kRowBytes / esz), (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)(row_bytes / esz), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   return fn(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base,
-            dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+            dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            row_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -573,6 +518,21 @@ int split_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
   if (a.obs_t0 && a.E > 0) gemm_obs_split(g, a.E, a.obs_out, st);
   if (cudaMemsetAsync(a.ctr, 0, sizeof(int), st) != cudaSuccess) return LGB_ERR_CUDA;
   if ((e = cudaGetLastError()) != cudaSuccess) return LGB_ERR_CUDA;
+  const int ps_grid = 8 * (NP / 64) * (NP / 64);
+  if (a.persist && sp.persist && a.D == 0 && !check && a.nt > 0 &&
+      (long long)a.nt * 8 * ps_grid < (1LL << 31)) {
+    // one persistent launch; its second operand copy starts as the first
+    const size_t esz = BF16 ? 2 : 4;
+    const size_t bytes = (size_t)2 * NP * sp.Wp * esz;
+    for (int l = 0; l < 2; ++l) {
+      if (cudaMemcpyAsync(static_cast<char*>(sp.Ls[l]) + bytes, sp.Ls[l], bytes, cudaMemcpyDeviceToDevice, st) !=
+              cudaSuccess ||
+          cudaMemcpyAsync(static_cast<char*>(sp.Rs[l]) + bytes, sp.Rs[l], bytes, cudaMemcpyDeviceToDevice, st) !=
+              cudaSuccess)
+        return LGB_ERR_CUDA;
+    }
+    return persist_propagate(a, st);
+  }
   // G1: T_k = L_k X, batched over k; G2: R = Ls . Rs^T
   CgArgs g1, g2;
   g1.p_row0 = 0;
@@ -653,8 +613,8 @@ int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_s
   // zero padding everywhere, then the static blocks
   const size_t esz = bf16 ? 2 : 4;
   for (int l = 0; l < 2; ++l) {
-    if (cudaMemsetAsync(sp.Ls[l], 0, (size_t)2 * NP * sp.Wp * esz, st) != cudaSuccess) return LGB_ERR_CUDA;
-    if (cudaMemsetAsync(sp.Rs[l], 0, (size_t)2 * NP * sp.Wp * esz, st) != cudaSuccess) return LGB_ERR_CUDA;
+    if (cudaMemsetAsync(sp.Ls[l], 0, (size_t)sp.copies * 2 * NP * sp.Wp * esz, st) != cudaSuccess) return LGB_ERR_CUDA;
+    if (cudaMemsetAsync(sp.Rs[l], 0, (size_t)sp.copies * 2 * NP * sp.Wp * esz, st) != cudaSuccess) return LGB_ERR_CUDA;
     if (Kd > 0 && cudaMemsetAsync(sp.Lks[l], 0, (size_t)Kd * 2 * NP * NP * esz, st) != cudaSuccess)
       return LGB_ERR_CUDA;
   }
@@ -697,6 +657,19 @@ int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_s
          make_map(&sp.map_g1[2], sp.Rs[0], bf16, 2LL * NP, sp.Wp, kQRows) &&
          make_map(&sp.map_g1[3], sp.Rs[1], bf16, 2LL * NP, sp.Wp, kQRows);
   if (!ok) return LGB_ERR_UNSUPPORTED;
+  // persistent kernel: boxes of 128 (Ls, Lks) and 64 (Rs) rows of 128 bytes,
+  // over both copies of Ls and Rs
+  sp.persist = false;
+  if (sp.copies == 2 && persist_supported(NP, bf16)) {
+    constexpr int RB = kPersistRowBytes;
+    sp.persist = make_map(&sp.map_ps[2], sp.Ls[0], bf16, 4LL * NP, sp.Wp, kPRows, RB) &&
+                 make_map(&sp.map_ps[3], sp.Ls[1], bf16, 4LL * NP, sp.Wp, kPRows, RB) &&
+                 make_map(&sp.map_ps[4], sp.Rs[0], bf16, 4LL * NP, sp.Wp, kPersistQRows, RB) &&
+                 make_map(&sp.map_ps[5], sp.Rs[1], bf16, 4LL * NP, sp.Wp, kPersistQRows, RB);
+    if (sp.persist && Kd > 0)
+      sp.persist = make_map(&sp.map_ps[0], sp.Lks[0], bf16, (long long)Kd * 2 * NP, NP, kPRows, RB) &&
+                   make_map(&sp.map_ps[1], sp.Lks[1], bf16, (long long)Kd * 2 * NP, NP, kPRows, RB);
+  }
   split_set_ksplit(sp, Kd, n_sm);
   const cudaError_t e = bf16 ? cudaFuncSetAttribute(cgemm3_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)kGemmSmem)

@@ -142,8 +142,13 @@ struct GemmSplit {
   float2* Rpart = nullptr;       // ks2 x NP x NP
   float2* kc = nullptr;          // N x N
   int ks1 = 1, ks2 = 1;
+  int copies = 1;                // 2: Ls and Rs hold a second copy (rows 2NP .. 4NP) for the persistent kernel
+  bool persist = false;          // the persistent kernel applies (NP <= 256, its clusters co-resident)
+  unsigned* bar = nullptr;       // persistent kernel: grid-barrier counter
+  double2* part = nullptr;       // persistent kernel: observable partials
   CUtensorMap map_g1[4];         // Lks hi, lo; Rs hi, lo
   CUtensorMap map_g2[4];         // Ls hi, lo; Rs hi, lo
+  CUtensorMap map_ps[6];         // persistent kernel: Lks hi, lo; Ls hi, lo; Rs hi, lo (both copies)
 };
 struct GemmRunArgs {
   GemmInstance g;
@@ -161,6 +166,7 @@ struct GemmRunArgs {
   double2* rho_out = nullptr;
   double2* states_out = nullptr;
   int graph_steps = 16;            // RK4 steps per captured CUDA graph
+  bool persist = true;             // split precision: the persistent kernel where it applies
   double check_tol = 0.0;          // per-step check (0: off)
   double* chk = nullptr;           // this instance's [2] check maxima
   double* chk_ws = nullptr;        // this instance's [8] check scratch
@@ -189,6 +195,11 @@ int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_s
 // split-K factors of one instance for a CTA budget (SM count x waves)
 void split_set_ksplit(GemmSplit& sp, int Kd, int cta_budget, int cap = 0);
 int split_propagate(const GemmRunArgs& a, cudaStream_t st);
+// persistent split-precision kernel (lgb_gemm_persist.cu): one launch for all
+// steps of a static instance with NP = 128 or 256
+bool persist_supported(int NP, bool bf16);
+int persist_part_elems(int NP);
+int persist_propagate(const GemmRunArgs& a, cudaStream_t st);
 
 }  // namespace lgb
 
@@ -212,6 +223,7 @@ struct lgb_plan {
   int opt_check = 0;                       // LGB_OPT_CHECK: 0 off, v: tolerance 10^-v
   int opt_kcap = 0;                        // LGB_OPT_GEMM_KSPLIT: split-K cap (0: none)
   int opt_gsteps = 16;                     // LGB_OPT_GRAPH_STEPS: RK4 steps per CUDA graph
+  int opt_persist = 1;                     // LGB_OPT_GEMM_PERSIST: persistent split kernel where it applies
   cudaStream_t cap_stream = nullptr;       // GEMM schedule: CUDA-graph capture
   int* d_ctr = nullptr;                    // GEMM schedule: device step counter
   void* blas_ws = nullptr;                 // cuBLAS workspace (graph capture allocates nothing)

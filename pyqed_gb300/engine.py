@@ -117,9 +117,11 @@ class Propagator:
 
     def set_option(self, name, value):
         """Option of the plan (``lgb_plan_set_option``): ``tc_pairs`` (0/1),
-        ``gemm_waves`` (1/2), ``check`` (0 off, v: the per-step trace and
-        hermiticity check at tolerance 10^-v), or the error-path test hook
-        ``test_stall`` (0/1)."""
+        ``gemm_waves`` (1/2), ``gemm_ksplit`` (split-K cap), ``graph_steps``
+        (RK4 steps per CUDA graph), ``gemm_persist`` (0/1: the persistent
+        split-precision kernel for 64 < N <= 256), ``check`` (0 off, v: the
+        per-step trace and hermiticity check at tolerance 10^-v), or the
+        error-path test hook ``test_stall`` (0/1)."""
         C.check(self._lib.lgb_plan_set_option(self._plan, C.OPT[name], int(value)),
                 "lgb_plan_set_option")
 
@@ -147,7 +149,8 @@ class Propagator:
         C.check(self._lib.lgb_plan_get_info(self._plan, ctypes.byref(inf)), "lgb_plan_get_info")
         return dict(schedule=C.SCHED_NAME[inf.schedule], precision=C.PREC_NAME[inf.precision],
                     smem_bytes=inf.smem_bytes, launches=inf.launches_per_propagate,
-                    workspace_bytes=inf.workspace_bytes, flops_per_step=inf.flops_per_step)
+                    workspace_bytes=inf.workspace_bytes, flops_per_step=inf.flops_per_step,
+                    persistent_instances=inf.persistent_instances)
 
     # -- helpers ---------------------------------------------------------------
     def to_device(self, host, pin=False):

@@ -37,11 +37,22 @@ def test_candidates():
 
 
 def test_gemm_candidates_cover_graph_length_and_split_k():
-    c = autotune.candidates([256], "3xtf32", "dense", 4)
+    c = autotune.candidates([1024], "3xtf32", "dense", 4)
     gemm = [x["options"] for x in c if x["schedule"] == "gemm"]
     assert {} in gemm and {"graph_steps": 32} in gemm
     assert {"gemm_waves": 2} in gemm and {"gemm_ksplit": 4} in gemm
     assert {"graph_steps": 32, "gemm_ksplit": 8} in gemm
+    assert all("gemm_persist" not in x for x in gemm)
+    # 64 < N <= 256, static: the persistent kernel (default) against the
+    # graph-replayed kernels, whose shapes are timed with it switched off
+    c = autotune.candidates([256], "3xbf16", "dense", 4)
+    gemm = [x["options"] for x in c if x["schedule"] == "gemm"]
+    assert gemm[0] == {} and {"gemm_persist": 0} in gemm
+    assert {"gemm_persist": 0, "graph_steps": 32, "gemm_ksplit": 8} in gemm
+    assert all(x.get("gemm_persist") == 0 for x in gemm[1:])
+    # driven instances never take the persistent kernel
+    c = autotune.candidates([256], "3xtf32", "dense", 4, n_drive=1)
+    assert all("gemm_persist" not in x["options"] for x in c)
     # the plain precisions have no split-K shape to tune
     c = autotune.candidates([256], "fp32", "dense", 4)
     assert all(set(x["options"]) <= {"graph_steps"} for x in c)

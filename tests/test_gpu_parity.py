@@ -454,6 +454,51 @@ def test_gemm_tuning_options_change_only_the_schedule():
             assert np.abs(r - out[()]).max() < tol, (prec, k)
 
 
+@pytest.mark.parametrize("prec", ["3xtf32", "3xbf16"])
+@pytest.mark.parametrize("N,K,kind", [(100, 3, "dense"), (128, 0, "none"), (129, 1, "dense"),
+                                      (160, 2, "dense"), (200, 2, "diag"), (256, 4, "dense"),
+                                      (250, 5, "dense")])
+def test_gemm_persistent_kernel_vs_oracle(prec, N, K, kind):
+    """The persistent split-precision kernel (one launch, clusters of 4 CTAs,
+    split-K partials summed through distributed shared memory) at both padded
+    sizes (NP = 128, 256) and every G1 split (K = 1: 4-way, 2: 2-way, 3 and 4:
+    one product per CTA, 5: two rounds), no collapse operators, diagonal ones;
+    observables with a t0 row, states stored every 3 steps: against the
+    complex128 oracle, and against the graph-replayed kernels of the same
+    precision (option gemm_persist = 0)."""
+    from pyqed_gb300.batch import prepare_batch
+    from pyqed_gb300.engine import Propagator
+    rng = np.random.default_rng(100 + N + K)
+    H, cops, rho0, O_ = _random_instance(rng, N, K)
+    if kind == "diag":
+        cops = [np.diag((rng.standard_normal(N) + 1j * rng.standard_normal(N)) * 0.1) for _ in range(K)]
+    nt, dt = 9, 0.02
+    obs, states = O.lindblad(H, rho0, cops, [O_, H], Nt=nt, dt=dt)
+    bi = prepare_batch([H], [cops], [rho0], [[O_, H]])
+    tol = TOL32 if prec == "3xtf32" else TOLBF
+    out = {}
+    for persist in (1, 0):
+        prop = Propagator(bi.dims, nt=nt, dt=dt, n_cops=bi.n_cops, cops_kind=bi.cops_kind, n_eops=2,
+                          precision=prec, schedule="gemm", store_every=3, obs_t0=True)
+        try:
+            prop.set_option("gemm_persist", persist)
+            prop.set_operators(bi.H, bi.cops, bi.eops, bi.dops)
+            assert prop.info()["persistent_instances"] == persist
+            o = prop.alloc_outputs(want_obs=True, want_rho=True, want_states=True)
+            prop.propagate_device(prop.to_device(bi.rho0), None, o)
+            prop.check_errors()
+            out[persist] = (prop.unpack_rho(o[1])[0], prop.unpack_obs(o[0])[0],
+                            prop.unpack_states(o[2])[0])
+        finally:
+            prop.close()
+    for persist, (rho, ob, st) in out.items():
+        assert np.abs(rho - states[-1]).max() < tol, persist
+        assert np.abs(ob - obs).max() < tol * N, persist
+        for k in range(nt // 3):
+            assert np.abs(st[k] - states[3 * k + 2]).max() < tol, (persist, k)
+    assert np.abs(out[1][0] - out[0][0]).max() < tol
+
+
 @pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32), ("3xtf32", TOL32)])
 def test_gemm_schedule_graph_replay_vs_oracle(prec, tol):
     """45 steps: two replays of a captured 16-step CUDA graph and one of a
