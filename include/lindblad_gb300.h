@@ -176,8 +176,8 @@ int lgb_plan_adjoint(lgb_plan_t plan, const double* rho0, const double* drive,
 /* Plan introspection: the schedule and precision in use, the bytes of
  * device workspace, the dynamic shared memory per CTA, the number of
  * kernel launches one propagate issues and the number of instances that a
- * propagate without the per-step check runs on the persistent split-precision
- * kernel (LGB_OPT_GEMM_PERSIST). */
+ * propagate runs on the persistent split-precision kernel
+ * (LGB_OPT_GEMM_PERSIST). */
 typedef struct {
   int32_t schedule;
   int32_t precision;
@@ -211,9 +211,8 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
  *   LGB_OPT_GEMM_PERSIST split-precision GEMM schedule: 1 (default) runs a
  *                      static instance with 64 < N <= 256 as one persistent
  *                      launch (clusters of 8 CTAs, two grid barriers per RK4
- *                      stage) when the device holds all its CTAs at once and
- *                      the per-step check is off; 0 always uses the graph-
- *                      replayed kernels
+ *                      stage) when the device holds all its CTAs at once;
+ *                      0 always uses the graph-replayed kernels
  *   LGB_OPT_CHECK      per-step check of the state, accumulated in FP64:
  *                      0 (default) off; v = 1..15 checks after every step
  *                      that |Tr rho(t) - Tr rho0| <= 10^-v and, for

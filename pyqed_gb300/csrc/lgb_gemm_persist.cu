@@ -158,11 +158,18 @@ struct PsArgs {
   const float2* Dm = nullptr;    // diagonal-collapse dissipator (diag)
   const double2* Ot = nullptr;   // E x N x N observables transposed
   double2* obs_out = nullptr;    // this instance's rows
-  double2* part = nullptr;       // [2][16][grid] observable partials
+  double2* part = nullptr;       // [2][kPsSlots][grid] observable and check partials
   unsigned* bar = nullptr;       // grid-barrier counter, zero at launch
   int* err = nullptr;
   StepOut so;
+  // per-step check (check_tol > 0): the state's trace drift and hermiticity
+  // deviation folded into chk[2] against the rho0 values in chk_ws[0..2]
+  double check_tol = 0.0;
+  double* chk = nullptr;
+  const double* chk_ws = nullptr;
 };
+
+constexpr int kPsSlots = 18;  // partial slots per step parity: 16 observables, trace, hermiticity
 
 template <bool BF16>
 __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads, 1)
@@ -173,6 +180,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   __shared__ uint32_t tmem_base;
   __shared__ int s_dead;
   __shared__ double s_red[4][16][2];
+  __shared__ double s_chk[4][3];
   constexpr int KT = kPsRowBytes / (BF16 ? 2 : 4);  // K elements per ring stage
   constexpr int KSTEPS = KT / (BF16 ? 16 : 8);      // MMA K-steps per ring stage (32 B each)
   constexpr uint32_t id = idesc(BF16 ? kFmtBF16 : kFmtTF32, 128, 2 * kPsCols, false, false);
@@ -339,6 +347,73 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   T* const RH = reinterpret_cast<T*>(a.Rs[0]);
   T* const RL = reinterpret_cast<T*>(a.Rs[1]);
   const float sixth = (float)(a.dt / 6.0);
+  const bool check = a.check_tol > 0.0;
+
+  // Per-step check of step `step`'s state: this CTA's elements against their
+  // transposes (the FP32 state every owner wrote at that step's last stage)
+  // and its share of the trace, into the partial slots of the step's parity.
+  auto check_partials = [&](int step) {
+    double h = 0.0, tx = 0.0, ty = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int ig = 64 * I + orow + (tid >> 5) + 4 * q, jg = kPsCols * J + ocol;
+      if (ig < N && jg < N) {
+        const float2 xt = a.rho[(long long)jg * N + ig];
+        h = fmax(h, hypot((double)rr[q].x - (double)xt.x, (double)rr[q].y + (double)xt.y));
+        if (ig == jg) {
+          tx += rr[q].x;
+          ty += rr[q].y;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+      tx += __shfl_xor_sync(0xffffffffu, tx, o);
+      ty += __shfl_xor_sync(0xffffffffu, ty, o);
+    }
+    if (lane == 0) {
+      s_chk[warp][0] = h;
+      s_chk[warp][1] = tx;
+      s_chk[warp][2] = ty;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      const double hh = fmax(fmax(s_chk[0][0], s_chk[1][0]), fmax(s_chk[2][0], s_chk[3][0]));
+      const double sx = (s_chk[0][1] + s_chk[1][1]) + (s_chk[2][1] + s_chk[3][1]);
+      const double sy = (s_chk[0][2] + s_chk[1][2]) + (s_chk[2][2] + s_chk[3][2]);
+      a.part[((long long)(step & 1) * kPsSlots + 16) * gridDim.x + blockIdx.x] = make_double2(sx, sy);
+      a.part[((long long)(step & 1) * kPsSlots + 17) * gridDim.x + blockIdx.x] = make_double2(hh, 0.0);
+    }
+  };
+  // (CTA 0, once every CTA's partials of `step` are in) fold into the maxima
+  auto check_fold = [&](int step) {
+    if (blockIdx.x != 0 || tid != 0) return;
+    const double2* pt = a.part + ((long long)(step & 1) * kPsSlots + 16) * gridDim.x;
+    const double2* ph = a.part + ((long long)(step & 1) * kPsSlots + 17) * gridDim.x;
+    double sx = 0.0, sy = 0.0, h = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) {
+      const volatile double* vt = reinterpret_cast<const volatile double*>(pt + b);
+      const volatile double* vh = reinterpret_cast<const volatile double*>(ph + b);
+      sx += vt[0];
+      sy += vt[1];
+      h = fmax(h, vh[0]);
+    }
+    const double dtr = hypot(sx - a.chk_ws[0], sy - a.chk_ws[1]);
+    a.chk[0] = fmax(a.chk[0], dtr);
+    bool bad = !(dtr <= a.check_tol);
+    if (a.chk_ws[2] != 0.0) {
+      a.chk[1] = fmax(a.chk[1], h);
+      bad = bad || !(h <= a.check_tol);
+    }
+    if (bad) atomicCAS(a.err, 0, 9);  // LGB_ERR_CHECK
+  };
+  int fold_step = -1;  // a step whose check partials await the fold after the next grid barrier
+  auto gsync_fold = [&]() {
+    gsync();
+    if (fold_step >= 0 && !dead) check_fold(fold_step);
+    fold_step = -1;
+  };
 
   // tile row i, column col of an owner's receive buffer (rows_per rows per source)
   auto roff = [](int src, int rows_per, int rl, int c, int i, int col) {
@@ -348,6 +423,10 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   for (int step = 0; step < a.nt; ++step) {
     for (int stage = 0; stage < 4; ++stage) {
       const int cp = stage & 1, nx = cp ^ 1;  // operand copy read / written by this stage
+      if (check && stage == 0 && step > 0 && !dead) {
+        check_partials(step - 1);
+        fold_step = step - 1;
+      }
       // ---- G1: T_k = L_k X, K products of the tile position split s1 ways ----------
       if (a.K > 0) {
         const int groups = kPsCluster / a.s1, g = rank / a.s1, zz = rank % a.s1;
@@ -386,7 +465,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
             }
           }
         }
-        gsync();
+        gsync_fold();
       }
       // ---- G2: R = Ls . Rs^T, the tile's K extent split over the cluster -----------
       if (!dead) {
@@ -464,6 +543,14 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
       }
       if (stage == 3 && !dead) {
         if (__syncthreads_or(!fin) && tid == 0) atomicCAS(a.err, 0, 4);  // LGB_ERR_NONFINITE
+        if (check) {
+          // the state of this step, for the transposed reads of its check
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int ig = 64 * I + orow + (tid >> 5) + 4 * q, jg = kPsCols * J + ocol;
+            if (ig < N && jg < N) a.rho[(long long)ig * N + jg] = rr[q];
+          }
+        }
         double2* state_out = a.so.state_at(step, (long long)N * N);
         double2* rho_out = step == a.nt - 1 ? a.so.rho_out : nullptr;
         if (state_out != nullptr || rho_out != nullptr) {
@@ -502,13 +589,13 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
         if (tid < a.E) {
           const double sx = (s_red[0][tid][0] + s_red[1][tid][0]) + (s_red[2][tid][0] + s_red[3][tid][0]);
           const double sy = (s_red[0][tid][1] + s_red[1][tid][1]) + (s_red[2][tid][1] + s_red[3][tid][1]);
-          a.part[((long long)(step & 1) * 16 + tid) * gridDim.x + blockIdx.x] = make_double2(sx, sy);
+          a.part[((long long)(step & 1) * kPsSlots + tid) * gridDim.x + blockIdx.x] = make_double2(sx, sy);
         }
       }
-      gsync();
+      gsync_fold();
       if (stage == 3 && !dead && blockIdx.x == 0 && tid < a.E) {
         // every CTA's partial of this step is in: fixed-order FP64 sum
-        const double2* pp = a.part + ((long long)(step & 1) * 16 + tid) * gridDim.x;
+        const double2* pp = a.part + ((long long)(step & 1) * kPsSlots + tid) * gridDim.x;
         double sx = 0.0, sy = 0.0;
         for (unsigned b = 0; b < gridDim.x; ++b) {
           const volatile double* vp = reinterpret_cast<const volatile double*>(pp + b);
@@ -518,6 +605,12 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
         a.obs_out[((long long)step + a.obs_t0) * a.E + tid] = make_double2(sx, sy);
       }
     }
+  }
+  if (check && a.nt > 0 && !dead) {
+    // the last step's check
+    check_partials(a.nt - 1);
+    fold_step = a.nt - 1;
+    gsync_fold();
   }
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -555,7 +648,7 @@ bool persist_supported(int NP, bool bf16) {
   return nc * kPsCluster >= grid_of(NP);
 }
 
-int persist_part_elems(int NP) { return 2 * 16 * grid_of(NP); }
+int persist_part_elems(int NP) { return 2 * kPsSlots * grid_of(NP); }
 
 int persist_propagate(const GemmRunArgs& a, cudaStream_t st) {
   const GemmSplit& sp = a.sp;
@@ -593,6 +686,11 @@ int persist_propagate(const GemmRunArgs& a, cudaStream_t st) {
   p.so.store_every = a.store_every;
   p.so.states_out = a.states_out;
   p.so.rho_out = a.rho_out;
+  if (a.check_tol > 0.0 && a.chk != nullptr) {
+    p.check_tol = a.check_tol;
+    p.chk = a.chk;
+    p.chk_ws = a.chk_ws;
+  }
   if (p.nkb2 < kPsCluster || (p.K > 0 && p.nkb1 < p.s1)) return LGB_ERR_UNSUPPORTED;
   PsMaps mp;
   mp.p1h = sp.map_ps[0];

@@ -519,7 +519,7 @@ int split_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
   if (cudaMemsetAsync(a.ctr, 0, sizeof(int), st) != cudaSuccess) return LGB_ERR_CUDA;
   if ((e = cudaGetLastError()) != cudaSuccess) return LGB_ERR_CUDA;
   const int ps_grid = 8 * (NP / 64) * (NP / 64);
-  if (a.persist && sp.persist && a.D == 0 && !check && a.nt > 0 &&
+  if (a.persist && sp.persist && a.D == 0 && a.nt > 0 &&
       (long long)a.nt * 8 * ps_grid < (1LL << 31)) {
     // one persistent launch; its second operand copy starts as the first
     const size_t esz = BF16 ? 2 : 4;

@@ -104,3 +104,41 @@ def test_solver_run_check_attribute(golden):
     # the oracle's own trace stays at 1 as well
     obs, states = O.lindblad(g["H"], g["rho0"], list(g["c_ops"]), list(g["e_ops"]), Nt=20, dt=float(g["dt"]))
     assert abs(np.trace(states[-1]) - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("prec", ["3xtf32", "3xbf16"])
+def test_check_on_the_persistent_kernel(prec):
+    """The persistent split-precision kernel (64 < N <= 256, static) runs the
+    per-step check itself: its results are bitwise those of an unchecked
+    run, its maxima agree with the graph-replayed kernels' check to
+    rounding, and a tolerance below rounding flags the instance."""
+    from pyqed_gb300.batch import prepare_batch
+    from pyqed_gb300.engine import Propagator
+    H, cops, rho0 = _hermitian_batch([200], 2, "dense", seed=7)
+    bi = prepare_batch(H, cops, rho0, [[h] for h in H])
+    out = {}
+    for persist, tol in ((1, None), (1, 1e-3), (0, 1e-3), (1, 1e-15)):
+        prop = Propagator(bi.dims, nt=40, dt=0.02, n_cops=bi.n_cops, cops_kind=bi.cops_kind, n_eops=1,
+                          precision=prec, schedule="gemm")
+        try:
+            prop.set_option("gemm_persist", persist)
+            prop.set_check(tol)
+            prop.set_operators(bi.H, bi.cops, bi.eops, bi.dops)
+            assert prop.info()["persistent_instances"] == persist
+            o = prop.alloc_outputs(want_obs=True, want_rho=True)
+            prop.propagate_device(prop.to_device(bi.rho0), None, o)
+            with warnings.catch_warnings(record=True):
+                warnings.simplefilter("always")
+                flags = prop.check_errors()
+            out[(persist, tol)] = (prop.unpack_rho(o[1])[0], prop.unpack_obs(o[0])[0], flags.copy(),
+                                   prop.check_stats()[0] if tol else None)
+        finally:
+            prop.close()
+    rho, obs, flags, _ = out[(1, None)]
+    for key in ((1, 1e-3), (1, 1e-15)):
+        assert np.array_equal(out[key][0], rho) and np.array_equal(out[key][1], obs)
+    assert (out[(1, 1e-3)][2] == 0).all() and (out[(0, 1e-3)][2] == 0).all()
+    assert (out[(1, 1e-15)][2] != 0).all()
+    st_p, st_g = out[(1, 1e-3)][3], out[(0, 1e-3)][3]
+    assert 0.0 <= st_p[0] < 1e-4 and 0.0 <= st_p[1] < 1e-4
+    assert np.all(np.abs(st_p - st_g) < 1e-5)
