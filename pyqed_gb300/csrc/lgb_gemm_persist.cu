@@ -13,7 +13,7 @@
 //   ((NP/64)(NP/32) clusters, 128 CTAs at NP = 256, one CTA per SM; clusters
 //   of 4 because a GB300 holds 15 clusters of 8 such CTAs, 36 of 4).  Every
 //   work item is an M = 128, N = 64 tcgen05 product (64 x 32 complex, the
-//   interleaved real form of lgb_tc.cu) over a K range, fed by a 3-stage TMA
+//   interleaved real form of lgb_tc.cu) over a K range, fed by a 4-stage TMA
 //   ring of 128-byte-swizzled rows (thread 0) and issued by one thread
 //   (thread 32) as the three leading split products hi*hi, hi*lo, lo*hi.
 // * G2: the 4 CTAs of a cluster split its tile's K extent (K + 2) NP four
@@ -58,15 +58,15 @@ constexpr int kPsThreads = 128;
 constexpr int kPsCluster = 4;
 constexpr int kPsCols = kPersistQRows / 2;               // complex columns of a tile (64 rows)
 constexpr int kPsOwn = 64 / kPsCluster;                  // G2 tile rows owned by one CTA
-constexpr int kPsStages = 3;
+constexpr int kPsStages = 4;
 constexpr int kPsRowBytes = kPersistRowBytes;            // K bytes per operand row and ring stage
 constexpr uint32_t kPsTileP = 128 * kPsRowBytes;         // 16 KB: one level of the M-side operand
 constexpr uint32_t kPsTileQ = 2 * kPsCols * kPsRowBytes; // 8 KB: one level of the N-side operand
 constexpr uint32_t kPsStageBytes = 2 * kPsTileP + 2 * kPsTileQ;  // P hi, P lo, Q hi, Q lo
-constexpr uint32_t kPsRing = kPsStages * kPsStageBytes;  // 144 KB
+constexpr uint32_t kPsRing = kPsStages * kPsStageBytes;  // 192 KB
 constexpr uint32_t kPsRecv = 64 * 2 * kPsCols * 4;       // 16 KB: tile rows x parts x columns, FP32
 constexpr uint32_t kPsXs = kPsOwn * kPsCols * sizeof(float2);  // 4 KB: the owner's next X rows
-constexpr uint32_t kPsSmem = kPsRing + 2 * kPsRecv + kPsXs + 1024;  // + alignment slack
+constexpr uint32_t kPsSmem = kPsRing + kPsRecv + kPsXs + 1024;  // + alignment slack (213 KB)
 constexpr unsigned long long kPsBarNs = 1000000000ull;   // grid-barrier wait bound (1 s)
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -193,9 +193,11 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   const uint32_t sraw = smem_u32(ps_smem);
   const uint32_t sb = (sraw + 1023u) & ~1023u;  // ring base (1 KB aligned for the swizzled tiles)
   unsigned char* gb = ps_smem + (sb - sraw);
-  const uint32_t recv = sb + kPsRing;           // two receive buffers, kPsRecv apart
+  // one receive buffer: its reuse by the next phase is ordered by the grid
+  // barrier between the phases
+  const uint32_t recv = sb + kPsRing;
   const float* recvf = reinterpret_cast<const float*>(gb + kPsRing);
-  float2* xs = reinterpret_cast<float2*>(gb + kPsRing + 2 * kPsRecv);
+  float2* xs = reinterpret_cast<float2*>(gb + kPsRing + kPsRecv);
 
   if (tid == 0) {
     for (int s = 0; s < kPsStages; ++s) {
@@ -227,7 +229,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
     ra[q] = kc[q] = make_float2(0.f, 0.f);
     xc[q] = rr[q];
   }
-  uint32_t kit = 0, nitem = 0, nred = 0, nbar = 0;
+  uint32_t kit = 0, nitem = 0, nbar = 0;
 
   // One product over ring stages [kb0, kb1) into the TMEM accumulator.
   auto item = [&](const CUtensorMap* ph, const CUtensorMap* pl, int prow, int qrow, int kb0, int kb1) {
@@ -287,7 +289,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   // chunks are stored at chunk ^ (i % 8), which spreads one store
   // instruction of a warp over the banks.
   auto push = [&](int src, int rows_per, int owner0) {
-    const uint32_t buf = recv + (nred & 1) * kPsRecv;
+    const uint32_t buf = recv;
     if (!mbar_wait(&done, nitem & 1, kGemmSpin)) atomicExch(a.err, 5);
     ++nitem;
     fence_after_sync();
@@ -315,6 +317,9 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
       st_cluster4(dst + 16u * (uint32_t)(q ^ sw), v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
   };
 
+  // Grid barrier: the CTA's writes are ordered before thread 0's release-add
+  // by the CTA barrier, and the acquire polls before the CTA's later reads by
+  // the second one (no separate fences: they cost 6 % of a step).
   auto gsync = [&]() {
     fence_proxy_global();
     __syncthreads();
@@ -322,7 +327,6 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
     if (tid == 0) {
       int d = s_dead;
       if (!d) {
-        __threadfence();
         red_release_add(a.bar, 1u);
         const unsigned target = nbar * gridDim.x;
         const unsigned long long t0 = gtimer();
@@ -333,7 +337,6 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
             break;
           }
         }
-        __threadfence();
         if (*reinterpret_cast<volatile int*>(a.err) == 5) d = 1;
       }
       s_dead = d;
@@ -440,8 +443,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
             push(zz, rows_per, g * a.s1);
           }
           cluster_sync_all();
-          const float* rb = recvf + (nred & 1) * (kPsRecv / 4);
-          ++nred;
+          const float* rb = recvf;
           if (act) {
             // owned rows [zz rows_per, +rows_per) of T_k -> M-side block 2 + k of this
             // copy, 8 columns of one row part per task
@@ -464,6 +466,8 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
               store8_split<BF16>(LH + row * Wp + colg, LL + row * Wp + colg, v);
             }
           }
+          // (one receive buffer: the next round's stores wait until every owner has read)
+          if (k0 + groups < a.K) cluster_sync_all();
         }
         gsync_fold();
       }
@@ -474,8 +478,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
         push(rank, kPsOwn, 0);
       }
       cluster_sync_all();
-      const float* rb = recvf + (nred & 1) * (kPsRecv / 4);
-      ++nred;
+      const float* rb = recvf;
       bool fin = true;
       if (!dead) {
         const float cst = (float)((stage == 2) ? a.dt : 0.5 * a.dt);
