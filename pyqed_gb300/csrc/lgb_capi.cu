@@ -336,14 +336,18 @@ int lgb_plan_create(lgb_plan_t* plan, const lgb_problem_t* problem, const int32_
         q.NP = lgb::split_padded_dim(pl->dims[b]);
         q.Wp = (long long)(Kd + 2) * q.NP;
         q.bf16 = bf16;
-        // (a second copy of Ls and Rs for the persistent kernel where it may apply)
-        q.copies = q.NP <= 256 ? 2 : 1;
         for (int l = 0; l < 2; ++l) {
-          s = s ? s : dalloc(pl, &q.Ls[l], (size_t)q.copies * 2 * q.NP * q.Wp * ses);
-          s = s ? s : dalloc(pl, &q.Rs[l], (size_t)q.copies * 2 * q.NP * q.Wp * ses);
+          s = s ? s : dalloc(pl, &q.Ls[l], (size_t)2 * q.NP * q.Wp * ses);
+          s = s ? s : dalloc(pl, &q.Rs[l], (size_t)2 * q.NP * q.Wp * ses);
           s = s ? s : dalloc(pl, &q.Lks[l], (size_t)Kd * 2 * q.NP * q.NP * ses);
         }
-        if (q.copies == 2) {
+        if (q.NP <= 256) {
+          // the persistent kernel's blocked operands (two copies of Ls and Rs)
+          for (int l = 0; l < 2; ++l) {
+            s = s ? s : dalloc(pl, &q.Lsb[l], (size_t)2 * 2 * q.NP * q.Wp * ses);
+            s = s ? s : dalloc(pl, &q.Rsb[l], (size_t)2 * 2 * q.NP * q.Wp * ses);
+            s = s ? s : dalloc(pl, &q.Lksb[l], (size_t)Kd * 2 * q.NP * q.NP * ses);
+          }
           s = s ? s : dalloc(pl, &q.bar, sizeof(unsigned));
           s = s ? s : dalloc(pl, &q.part, (size_t)lgb::persist_part_elems(q.NP) * sizeof(double2));
         }

@@ -56,10 +56,10 @@ using namespace splitk;
 
 constexpr int kPsThreads = 128;
 constexpr int kPsCluster = 4;
-constexpr int kPsCols = kPersistQRows / 2;               // complex columns of a tile (64 rows)
+constexpr int kPsCols = 32;                              // complex columns of a tile (64 rows)
 constexpr int kPsOwn = 64 / kPsCluster;                  // G2 tile rows owned by one CTA
 constexpr int kPsStages = 4;
-constexpr int kPsRowBytes = kPersistRowBytes;            // K bytes per operand row and ring stage
+constexpr int kPsRowBytes = 128;                         // K bytes per operand row and ring stage
 constexpr uint32_t kPsTileP = 128 * kPsRowBytes;         // 16 KB: one level of the M-side operand
 constexpr uint32_t kPsTileQ = 2 * kPsCols * kPsRowBytes; // 8 KB: one level of the N-side operand
 constexpr uint32_t kPsStageBytes = 2 * kPsTileP + 2 * kPsTileQ;  // P hi, P lo, Q hi, Q lo
@@ -141,19 +141,59 @@ __device__ __forceinline__ void store8_split(typename SElem<BF16>::T* hd, typena
   }
 }
 
-struct PsMaps {
-  CUtensorMap p1h, p1l;  // G1 M side: the L_k rows (K x 2NP rows, pitch NP)
-  CUtensorMap p2h, p2l;  // G2 M side: Ls, both copies (4NP rows, pitch Wp)
-  CUtensorMap qh, ql;    // N side of both: Rs, both copies (4NP rows, pitch Wp, 64-row boxes)
-};
+// Blocked operand layout: an operand of R rows and K columns is stored as
+// 64-row x 128-byte blocks, block (row block rb, K block kb) at position
+// kb * nrb + rb (nrb = R / 64), each laid out as the 128-byte-swizzled
+// K-major shared-memory tile (row r at r * 128 B, 16-byte chunk c at chunk
+// c ^ (r % 8)).  A 128-row M-side tile of one K block is then 16 KB and a
+// 64-row N-side tile 8 KB of contiguous memory, one bulk copy each.
+template <int ESZ>
+__device__ __forceinline__ long long boff(int r, long long k, int nrb) {
+  constexpr int KT = kPsRowBytes / ESZ, CE = 16 / ESZ;  // elements per block row, per chunk
+  const long long kb = k / KT;
+  const int kk = (int)(k - kb * KT);
+  return ((kb * nrb + (r >> 6)) * 64 + (r & 63)) * KT + ((kk / CE) ^ (r & 7)) * CE + kk % CE;
+}
+
+// 8 consecutive values of row r from column k (a multiple of 8) -> hi and lo
+// blocked arrays (one 16-byte chunk at BF16, two at TF32)
+template <bool BF16>
+__device__ __forceinline__ void store8_blk(typename SElem<BF16>::T* H, typename SElem<BF16>::T* L, int r,
+                                           long long k, int nrb, const float* v) {
+  constexpr int ESZ = BF16 ? 2 : 4;
+  if constexpr (BF16) {
+    const long long o = boff<ESZ>(r, k, nrb);
+    store8_split<true>(H + o, L + o, v);
+  } else {
+    float h[4], l[4];
+    for (int half = 0; half < 2; ++half) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) SElem<false>::split(v[4 * half + u], h[u], l[u]);
+      const long long o = boff<ESZ>(r, k + 4 * half, nrb);
+      *reinterpret_cast<uint4*>(H + o) =
+          make_uint4(__float_as_uint(h[0]), __float_as_uint(h[1]), __float_as_uint(h[2]), __float_as_uint(h[3]));
+      *reinterpret_cast<uint4*>(L + o) =
+          make_uint4(__float_as_uint(l[0]), __float_as_uint(l[1]), __float_as_uint(l[2]), __float_as_uint(l[3]));
+    }
+  }
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+               : "memory");
+}
 
 struct PsArgs {
   int N = 0, NP = 0, K = 0, E = 0, nt = 0, diag = 0, obs_t0 = 0;
   int s1 = 1, nkb1 = 0, nkb2 = 0, tn = 0;  // tn: column tiles (NP / 32)
   long long Wp = 0;
   double dt = 0.0;
-  void* Ls[2] = {nullptr, nullptr};
-  void* Rs[2] = {nullptr, nullptr};
+  const void* Lks[2] = {nullptr, nullptr};  // blocked operands (hi, lo): L_k rows (nrb1 row blocks)
+  void* Ls[2] = {nullptr, nullptr};         // Ls, two copies of copy_elems (nrb2 row blocks each)
+  void* Rs[2] = {nullptr, nullptr};         // Rs, the same
+  int nrb1 = 0, nrb2 = 0;
+  long long copy_elems = 0;
   float2* rho = nullptr;         // FP32 state (read at the start, written at the end)
   const float2* Dm = nullptr;    // diagonal-collapse dissipator (diag)
   const double2* Ot = nullptr;   // E x N x N observables transposed
@@ -173,7 +213,7 @@ constexpr int kPsSlots = 18;  // partial slots per step parity: 16 observables, 
 
 template <bool BF16>
 __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads, 1)
-    persist_rk4_kernel(const __grid_constant__ PsMaps m, const PsArgs a) {
+    persist_rk4_kernel(const PsArgs a) {
   using T = typename SElem<BF16>::T;
   extern __shared__ unsigned char ps_smem[];
   __shared__ uint64_t full[kPsStages], empty[kPsStages], done;
@@ -189,7 +229,6 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   const int cid = (int)cluster_idx();
   const int I = cid / a.tn, J = cid % a.tn;  // the cluster's G2 tile
   const int N = a.N, NP = a.NP;
-  const long long Wp = a.Wp;
   const uint32_t sraw = smem_u32(ps_smem);
   const uint32_t sb = (sraw + 1023u) & ~1023u;  // ring base (1 KB aligned for the swizzled tiles)
   unsigned char* gb = ps_smem + (sb - sraw);
@@ -231,8 +270,11 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   }
   uint32_t kit = 0, nitem = 0, nbar = 0;
 
-  // One product over ring stages [kb0, kb1) into the TMEM accumulator.
-  auto item = [&](const CUtensorMap* ph, const CUtensorMap* pl, int prow, int qrow, int kb0, int kb1) {
+  // One product over ring stages [kb0, kb1) into the TMEM accumulator: the
+  // M-side blocks from P (row block rbp of nrbp), the N-side from Q (row
+  // block rbq of nrb2), hi and lo.
+  auto item = [&](const T* ph, const T* pl, int rbp, int nrbp, const T* qh, const T* ql, int rbq, int kb0,
+                  int kb1) {
     if (tid == 0) {
       fence_proxy_global();
       bool ok = true;
@@ -245,11 +287,12 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
         }
         mbar_expect_tx(&full[s], kPsStageBytes);
         const uint32_t st = sb + s * kPsStageBytes;
-        const int x = kb * KT;
-        tma_load_2d(st, ph, x, prow, &full[s]);
-        tma_load_2d(st + kPsTileP, pl, x, prow, &full[s]);
-        tma_load_2d(st + 2 * kPsTileP, &m.qh, x, qrow, &full[s]);
-        tma_load_2d(st + 2 * kPsTileP + kPsTileQ, &m.ql, x, qrow, &full[s]);
+        const long long po = ((long long)kb * nrbp + rbp) * 64 * KT;
+        const long long qo = ((long long)kb * a.nrb2 + rbq) * 64 * KT;
+        bulk_load(st, ph + po, kPsTileP, &full[s]);
+        bulk_load(st + kPsTileP, pl + po, kPsTileP, &full[s]);
+        bulk_load(st + 2 * kPsTileP, qh + qo, kPsTileQ, &full[s]);
+        bulk_load(st + 2 * kPsTileP + kPsTileQ, ql + qo, kPsTileQ, &full[s]);
       }
       if (!ok) atomicExch(a.err, 5);  // LGB_ERR_TIMEOUT
     } else if (tid == 32) {
@@ -349,6 +392,9 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   T* const LL = reinterpret_cast<T*>(a.Ls[1]);
   T* const RH = reinterpret_cast<T*>(a.Rs[0]);
   T* const RL = reinterpret_cast<T*>(a.Rs[1]);
+  const T* const KH = reinterpret_cast<const T*>(a.Lks[0]);
+  const T* const KL = reinterpret_cast<const T*>(a.Lks[1]);
+  const long long CE = a.copy_elems;
   const float sixth = (float)(a.dt / 6.0);
   const bool check = a.check_tol > 0.0;
 
@@ -438,7 +484,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
           const int k = k0 + g;
           const bool act = k < a.K && !dead;
           if (act) {
-            item(&m.p1h, &m.p1l, k * 2 * NP + 128 * I, cp * 2 * NP + 2 * kPsCols * J,
+            item(KH, KL, (k * 2 * NP + 128 * I) / 64, a.nrb1, RH + cp * CE, RL + cp * CE, J,
                  zz * a.nkb1 / a.s1, (zz + 1) * a.nkb1 / a.s1);
             push(zz, rows_per, g * a.s1);
           }
@@ -461,9 +507,8 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
                 v[0] += lo4.x, v[1] += lo4.y, v[2] += lo4.z, v[3] += lo4.w;
                 v[4] += hi4.x, v[5] += hi4.y, v[6] += hi4.z, v[7] += hi4.w;
               }
-              const long long row = (long long)cp * 2 * NP + mrow(c, 64 * I + i);
               const long long colg = (long long)(2 + k) * NP + kPsCols * J + 8 * oct;
-              store8_split<BF16>(LH + row * Wp + colg, LL + row * Wp + colg, v);
+              store8_blk<BF16>(LH + cp * CE, LL + cp * CE, mrow(c, 64 * I + i), colg, a.nrb2, v);
             }
           }
           // (one receive buffer: the next round's stores wait until every owner has read)
@@ -473,7 +518,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
       }
       // ---- G2: R = Ls . Rs^T, the tile's K extent split over the cluster -----------
       if (!dead) {
-        item(&m.p2h, &m.p2l, cp * 2 * NP + 128 * I, cp * 2 * NP + 2 * kPsCols * J,
+        item(LH + cp * CE, LL + cp * CE, 2 * I, a.nrb2, RH + cp * CE, RL + cp * CE, J,
              rank * a.nkb2 / kPsCluster, (rank + 1) * a.nkb2 / kPsCluster);
         push(rank, kPsOwn, 0);
       }
@@ -520,7 +565,6 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
         // N-side block 0 (X^T) of the next copy: row (p, j), 8 of the owner's 16 columns
         {
           const int p = (tid >> 5) & 1, col = tid & 31, half = tid >> 6;
-          const long long row = (long long)nx * 2 * NP + ncol(p, kPsCols * J + col);
           const long long c0 = 64LL * I + orow + 8 * half;
           float v[8];
 #pragma unroll
@@ -528,12 +572,11 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
             const float2 x = xs[(8 * half + r) * kPsCols + col];
             v[r] = p == 0 ? x.x : x.y;
           }
-          store8_split<BF16>(RH + row * Wp + c0, RL + row * Wp + c0, v);
+          store8_blk<BF16>(RH + nx * CE, RL + nx * CE, ncol(p, kPsCols * J + col), c0, a.nrb2, v);
         }
         // M-side block 1 (X rows) of the next copy: row (c, i), 8 of the tile's 32 columns
         {
           const int oct = tid & 3, c = (tid >> 2) & 1, r = tid >> 3;
-          const long long row = (long long)nx * 2 * NP + mrow(c, 64 * I + orow + r);
           const long long c0 = (long long)NP + kPsCols * J + 8 * oct;
           float v[8];
 #pragma unroll
@@ -541,7 +584,7 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
             const float2 x = xs[r * kPsCols + 8 * oct + u];
             v[u] = c == 0 ? x.x : x.y;
           }
-          store8_split<BF16>(LH + row * Wp + c0, LL + row * Wp + c0, v);
+          store8_blk<BF16>(LH + nx * CE, LL + nx * CE, mrow(c, 64 * I + orow + r), c0, a.nrb2, v);
         }
       }
       if (stage == 3 && !dead) {
@@ -626,6 +669,31 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
   if (warp == 0) tmem_dealloc(tmem, 2 * kPsCols);
 }
 
+// K-major hi/lo arrays (rows x pitch elements) -> the blocked layout, into
+// `copies` copies copy_elems apart; one 16-byte chunk per thread and step.
+template <bool BF16>
+__global__ void to_blocks_kernel(const void* src_h, const void* src_l, long long rows, long long pitch,
+                                 void* dst_h, void* dst_l, int nrb, long long copy_elems, int copies) {
+  using T = typename SElem<BF16>::T;
+  constexpr int CE = 16 / (int)sizeof(T);
+  const long long cpr = pitch / CE, n = rows * cpr;
+  const T* sh = reinterpret_cast<const T*>(src_h);
+  const T* sl = reinterpret_cast<const T*>(src_l);
+  T* dh = reinterpret_cast<T*>(dst_h);
+  T* dl = reinterpret_cast<T*>(dst_l);
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long r = idx / cpr, k = (idx - r * cpr) * CE;
+    const uint4 vh = *reinterpret_cast<const uint4*>(sh + r * pitch + k);
+    const uint4 vl = *reinterpret_cast<const uint4*>(sl + r * pitch + k);
+    const long long o = boff<(int)sizeof(T)>((int)r, k, nrb);
+    for (int c = 0; c < copies; ++c) {
+      *reinterpret_cast<uint4*>(dh + c * copy_elems + o) = vh;
+      *reinterpret_cast<uint4*>(dl + c * copy_elems + o) = vl;
+    }
+  }
+}
+
 int grid_of(int NP) { return kPsCluster * (NP / 64) * (NP / kPsCols); }
 
 }  // namespace
@@ -673,9 +741,13 @@ int persist_propagate(const GemmRunArgs& a, cudaStream_t st) {
   p.tn = NP / kPsCols;
   p.Wp = sp.Wp;
   p.dt = a.dt;
+  p.nrb1 = a.Kdense * 2 * NP / 64;
+  p.nrb2 = 2 * NP / 64;
+  p.copy_elems = 2LL * NP * sp.Wp;
   for (int l = 0; l < 2; ++l) {
-    p.Ls[l] = sp.Ls[l];
-    p.Rs[l] = sp.Rs[l];
+    p.Lks[l] = sp.Lksb[l];
+    p.Ls[l] = sp.Lsb[l];
+    p.Rs[l] = sp.Rsb[l];
   }
   p.rho = reinterpret_cast<float2*>(a.g.rho);
   p.Dm = reinterpret_cast<const float2*>(a.g.Dm);
@@ -694,20 +766,34 @@ int persist_propagate(const GemmRunArgs& a, cudaStream_t st) {
     p.chk = a.chk;
     p.chk_ws = a.chk_ws;
   }
-  if (p.nkb2 < kPsCluster || (p.K > 0 && p.nkb1 < p.s1)) return LGB_ERR_UNSUPPORTED;
-  PsMaps mp;
-  mp.p1h = sp.map_ps[0];
-  mp.p1l = sp.map_ps[1];
-  mp.p2h = sp.map_ps[2];
-  mp.p2l = sp.map_ps[3];
-  mp.qh = sp.map_ps[4];
-  mp.ql = sp.map_ps[5];
+  const int grid = grid_of(NP);
+  if (p.nkb2 < kPsCluster || (p.K > 0 && p.nkb1 < p.s1) || (long long)a.nt * 9 * grid >= (1LL << 31))
+    return LGB_ERR_UNSUPPORTED;
+  // the operands (set up and initialised in the K-major arrays) into the
+  // blocked layout: L_k once, Ls and Rs into both copies
+  const int cgrid = 8 * 152;
+  if (sp.bf16) {
+    if (p.K > 0)
+      to_blocks_kernel<true><<<cgrid, 256, 0, st>>>(sp.Lks[0], sp.Lks[1], (long long)p.K * 2 * NP, NP, sp.Lksb[0],
+                                                    sp.Lksb[1], p.nrb1, 0, 1);
+    to_blocks_kernel<true><<<cgrid, 256, 0, st>>>(sp.Ls[0], sp.Ls[1], 2LL * NP, sp.Wp, sp.Lsb[0], sp.Lsb[1], p.nrb2,
+                                                  p.copy_elems, 2);
+    to_blocks_kernel<true><<<cgrid, 256, 0, st>>>(sp.Rs[0], sp.Rs[1], 2LL * NP, sp.Wp, sp.Rsb[0], sp.Rsb[1], p.nrb2,
+                                                  p.copy_elems, 2);
+  } else {
+    if (p.K > 0)
+      to_blocks_kernel<false><<<cgrid, 256, 0, st>>>(sp.Lks[0], sp.Lks[1], (long long)p.K * 2 * NP, NP, sp.Lksb[0],
+                                                     sp.Lksb[1], p.nrb1, 0, 1);
+    to_blocks_kernel<false><<<cgrid, 256, 0, st>>>(sp.Ls[0], sp.Ls[1], 2LL * NP, sp.Wp, sp.Lsb[0], sp.Lsb[1], p.nrb2,
+                                                   p.copy_elems, 2);
+    to_blocks_kernel<false><<<cgrid, 256, 0, st>>>(sp.Rs[0], sp.Rs[1], 2LL * NP, sp.Wp, sp.Rsb[0], sp.Rsb[1], p.nrb2,
+                                                   p.copy_elems, 2);
+  }
   if (cudaMemsetAsync(sp.bar, 0, sizeof(unsigned), st) != cudaSuccess) return LGB_ERR_CUDA;
-  const dim3 grid(grid_of(NP));
   if (sp.bf16)
-    persist_rk4_kernel<true><<<grid, kPsThreads, kPsSmem, st>>>(mp, p);
+    persist_rk4_kernel<true><<<grid, kPsThreads, kPsSmem, st>>>(p);
   else
-    persist_rk4_kernel<false><<<grid, kPsThreads, kPsSmem, st>>>(mp, p);
+    persist_rk4_kernel<false><<<grid, kPsThreads, kPsSmem, st>>>(p);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 

@@ -458,19 +458,16 @@ EncodeFn encode_fn() {
 
 // 2D map over a K-major split array (rows x pitch elements), box = 64 bytes x
 // box_rows, 64-byte swizzle.
-// (row_bytes 128: the 128-byte swizzle of the persistent kernel)
-bool make_map(CUtensorMap* m, void* base, bool bf16, long long rows, long long pitch, int box_rows,
-              int row_bytes = kRowBytes) {
+bool make_map(CUtensorMap* m, void* base, bool bf16, long long rows, long long pitch, int box_rows) {
   EncodeFn fn = encode_fn();
   if (fn == nullptr) return false;
   const int esz = bf16 ? 2 : 4;
   cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(pitch * esz)};
-  cuuint32_t box[2] = {(cuuint32_t)(row_bytes / esz), (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)(kRowBytes / esz), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   return fn(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base,
-            dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            row_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+            dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -518,20 +515,10 @@ int split_propagate_t(const GemmRunArgs& a, cudaStream_t st) {
   if (a.obs_t0 && a.E > 0) gemm_obs_split(g, a.E, a.obs_out, st);
   if (cudaMemsetAsync(a.ctr, 0, sizeof(int), st) != cudaSuccess) return LGB_ERR_CUDA;
   if ((e = cudaGetLastError()) != cudaSuccess) return LGB_ERR_CUDA;
-  const int ps_grid = 8 * (NP / 64) * (NP / 64);
-  if (a.persist && sp.persist && a.D == 0 && a.nt > 0 &&
-      (long long)a.nt * 8 * ps_grid < (1LL << 31)) {
-    // one persistent launch; its second operand copy starts as the first
-    const size_t esz = BF16 ? 2 : 4;
-    const size_t bytes = (size_t)2 * NP * sp.Wp * esz;
-    for (int l = 0; l < 2; ++l) {
-      if (cudaMemcpyAsync(static_cast<char*>(sp.Ls[l]) + bytes, sp.Ls[l], bytes, cudaMemcpyDeviceToDevice, st) !=
-              cudaSuccess ||
-          cudaMemcpyAsync(static_cast<char*>(sp.Rs[l]) + bytes, sp.Rs[l], bytes, cudaMemcpyDeviceToDevice, st) !=
-              cudaSuccess)
-        return LGB_ERR_CUDA;
-    }
-    return persist_propagate(a, st);
+  if (a.persist && sp.persist && a.D == 0 && a.nt > 0) {
+    // one persistent launch (after converting the operands into its blocked layout)
+    const int r = persist_propagate(a, st);
+    if (r != LGB_ERR_UNSUPPORTED) return r;
   }
   // G1: T_k = L_k X, batched over k; G2: R = Ls . Rs^T
   CgArgs g1, g2;
@@ -613,8 +600,8 @@ int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_s
   // zero padding everywhere, then the static blocks
   const size_t esz = bf16 ? 2 : 4;
   for (int l = 0; l < 2; ++l) {
-    if (cudaMemsetAsync(sp.Ls[l], 0, (size_t)sp.copies * 2 * NP * sp.Wp * esz, st) != cudaSuccess) return LGB_ERR_CUDA;
-    if (cudaMemsetAsync(sp.Rs[l], 0, (size_t)sp.copies * 2 * NP * sp.Wp * esz, st) != cudaSuccess) return LGB_ERR_CUDA;
+    if (cudaMemsetAsync(sp.Ls[l], 0, (size_t)2 * NP * sp.Wp * esz, st) != cudaSuccess) return LGB_ERR_CUDA;
+    if (cudaMemsetAsync(sp.Rs[l], 0, (size_t)2 * NP * sp.Wp * esz, st) != cudaSuccess) return LGB_ERR_CUDA;
     if (Kd > 0 && cudaMemsetAsync(sp.Lks[l], 0, (size_t)Kd * 2 * NP * NP * esz, st) != cudaSuccess)
       return LGB_ERR_CUDA;
   }
@@ -657,19 +644,8 @@ int split_setup(GemmSplit& sp, const GemmInstance& g, int Kd, bool bf16, int n_s
          make_map(&sp.map_g1[2], sp.Rs[0], bf16, 2LL * NP, sp.Wp, kQRows) &&
          make_map(&sp.map_g1[3], sp.Rs[1], bf16, 2LL * NP, sp.Wp, kQRows);
   if (!ok) return LGB_ERR_UNSUPPORTED;
-  // persistent kernel: boxes of 128 (Ls, Lks) and 64 (Rs) rows of 128 bytes,
-  // over both copies of Ls and Rs
-  sp.persist = false;
-  if (sp.copies == 2 && persist_supported(NP, bf16)) {
-    constexpr int RB = kPersistRowBytes;
-    sp.persist = make_map(&sp.map_ps[2], sp.Ls[0], bf16, 4LL * NP, sp.Wp, kPRows, RB) &&
-                 make_map(&sp.map_ps[3], sp.Ls[1], bf16, 4LL * NP, sp.Wp, kPRows, RB) &&
-                 make_map(&sp.map_ps[4], sp.Rs[0], bf16, 4LL * NP, sp.Wp, kPersistQRows, RB) &&
-                 make_map(&sp.map_ps[5], sp.Rs[1], bf16, 4LL * NP, sp.Wp, kPersistQRows, RB);
-    if (sp.persist && Kd > 0)
-      sp.persist = make_map(&sp.map_ps[0], sp.Lks[0], bf16, (long long)Kd * 2 * NP, NP, kPRows, RB) &&
-                   make_map(&sp.map_ps[1], sp.Lks[1], bf16, (long long)Kd * 2 * NP, NP, kPRows, RB);
-  }
+  // persistent kernel: blocked operands allocated and its clusters co-resident
+  sp.persist = sp.Lsb[0] != nullptr && persist_supported(NP, bf16);
   split_set_ksplit(sp, Kd, n_sm);
   const cudaError_t e = bf16 ? cudaFuncSetAttribute(cgemm3_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)kGemmSmem)

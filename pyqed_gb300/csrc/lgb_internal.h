@@ -142,13 +142,16 @@ struct GemmSplit {
   float2* Rpart = nullptr;       // ks2 x NP x NP
   float2* kc = nullptr;          // N x N
   int ks1 = 1, ks2 = 1;
-  int copies = 1;                // 2: Ls and Rs hold a second copy (rows 2NP .. 4NP) for the persistent kernel
-  bool persist = false;          // the persistent kernel applies (NP <= 256, its clusters co-resident)
-  unsigned* bar = nullptr;       // persistent kernel: grid-barrier counter
-  double2* part = nullptr;       // persistent kernel: observable partials
+  // persistent kernel (NP <= 256): the same operands in 64-row x 128-byte
+  // blocks laid out as the swizzled shared-memory tiles, Ls and Rs twice
+  bool persist = false;          // it applies (its clusters co-resident)
+  void* Lsb[2] = {nullptr, nullptr};
+  void* Rsb[2] = {nullptr, nullptr};
+  void* Lksb[2] = {nullptr, nullptr};
+  unsigned* bar = nullptr;       // grid-barrier counter
+  double2* part = nullptr;       // observable and check partials
   CUtensorMap map_g1[4];         // Lks hi, lo; Rs hi, lo
   CUtensorMap map_g2[4];         // Ls hi, lo; Rs hi, lo
-  CUtensorMap map_ps[6];         // persistent kernel: Lks hi, lo; Ls hi, lo; Rs hi, lo (both copies)
 };
 struct GemmRunArgs {
   GemmInstance g;

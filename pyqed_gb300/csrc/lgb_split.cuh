@@ -14,10 +14,7 @@ namespace splitk {
 using namespace umma;
 
 constexpr int kRowBytes = 64;  // K bytes per row and pipeline stage (one 64-byte swizzle atom)
-// N-side rows of one item of the persistent kernel (32 complex columns) and
-// its K bytes per row and pipeline stage (one 128-byte swizzle atom)
-constexpr int kPersistQRows = 64;
-constexpr int kPersistRowBytes = 128;
+
 // Poll bound of the pipeline waits: far above a tile's main loop (< 1 ms), far
 // below a stuck GPU.
 constexpr long long kGemmSpin = 1LL << 22;
