@@ -13,9 +13,10 @@
 //   ((NP/64)(NP/32) clusters, 128 CTAs at NP = 256, one CTA per SM; clusters
 //   of 4 because a GB300 holds 15 clusters of 8 such CTAs, 36 of 4).  Every
 //   work item is an M = 128, N = 64 tcgen05 product (64 x 32 complex, the
-//   interleaved real form of lgb_tc.cu) over a K range, fed by a 4-stage TMA
-//   ring of 128-byte-swizzled rows (thread 0) and issued by one thread
-//   (thread 32) as the three leading split products hi*hi, hi*lo, lo*hi.
+//   interleaved real form of lgb_tc.cu) over a K range, fed by a 4-stage
+//   ring of bulk copies from the blocked operand layout below (thread 0) and
+//   issued by one thread (thread 32) as the three leading split products
+//   hi*hi, hi*lo, lo*hi.
 // * G2: the 4 CTAs of a cluster split its tile's K extent (K + 2) NP four
 //   ways; G1: they take the K products of the tile position, each split
 //   s1 = 4 / K ways (rounded down to a power of two).  The split partials
@@ -28,9 +29,10 @@
 //   registers for the whole run; it applies the stage combination, writes
 //   the next stage input into both split operand layouts and, after stage 3,
 //   the observables' partials, the stored states and the final rho.
-// * The operand arrays hold two copies (rows [0, 2NP) and [2NP, 4NP)); stage
-//   s reads copy s % 2 and writes the next X into the other copy, so no CTA
-//   overwrites an operand that another CTA may still be loading.
+// * The operands live in blocked copies of the K-major split arrays (see
+//   boff), converted at launch; Ls and Rs have two copies: stage s reads
+//   copy s % 2 and writes the next X into the other, so no CTA overwrites an
+//   operand that another CTA may still be loading.
 //
 // Every mbarrier wait and every grid-barrier wait is bounded (a grid barrier
 // gives up after 1 s of global-timer time).  A wait that runs out sets
