@@ -407,6 +407,8 @@ int lgb_plan_set_operators(lgb_plan_t plan, const double* H, const double* cops,
   sp.n_eops = pr.n_eops;
   sp.n_drive = pr.n_drive;
   sp.padc = plan->padc;
+  sp.max_npad = 0;
+  for (int np_ : plan->npad) sp.max_npad = std::max(sp.max_npad, np_);
   sp.dims = plan->d_dims;
   sp.npad = plan->d_npad;
   sp.off = plan->d_off;

@@ -65,6 +65,7 @@ cudaError_t launch_adjoint_finish(const AdjParams& p, const long long* off, doub
 // ---- operator preparation (lgb_setup.cu) -------------------------------------
 struct SetupParams {
   int n_inst, n_cops, cops_kind, n_eops, n_drive, padc;
+  int max_npad;  // the largest padded dimension (sizes the setup grid)
   const int* dims;
   const int* npad;
   const long long* off;

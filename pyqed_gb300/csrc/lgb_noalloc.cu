@@ -186,6 +186,7 @@ extern "C" int lgb_propagate_noalloc(const double* H, int32_t n, const double* c
   sp.n_eops = n_eops;
   sp.n_drive = 0;
   sp.padc = 1;
+  sp.max_npad = NP;
   sp.dims = &t->dims;
   sp.npad = &t->npad;
   sp.off = &t->off;

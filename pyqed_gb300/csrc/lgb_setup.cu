@@ -11,6 +11,8 @@
 //   Dm  = sum_k l_k l_k^dag (entrywise)      diagonal collapse operators
 //   Gt  = (i H_d)^T                          drive terms (H(t) = H0 - f H_d)
 //   Ot  = O_e^T (FP64)                       observables
+#include <algorithm>
+
 #include "lgb_internal.h"
 
 namespace lgb {
@@ -129,7 +131,10 @@ cudaError_t launch_setup(const SetupParams& p, int precision, cudaStream_t strea
   trace_shift_kernel<<<p.n_inst, 256, 0, stream>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  dim3 grid(64, p.n_inst);
+  // blocks per instance: enough for the largest padded matrix, at most 64
+  const long long ms = (long long)p.max_npad * (p.max_npad + p.padc);
+  const int gx = (int)std::max<long long>(1, std::min<long long>(64, (ms + 255) / 256));
+  dim3 grid(gx, p.n_inst);
   if (precision == 0) {
     setup_kernel<double><<<grid, 256, 0, stream>>>(p);
   } else {
