@@ -108,7 +108,7 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-// order this thread's generic global writes before later async-proxy (TMA) reads
+// order this thread's generic global writes before later async-proxy (bulk copy) reads
 __device__ __forceinline__ void fence_proxy_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
 // hi and lo parts of 8 consecutive values -> 16-byte-aligned vector stores
@@ -189,7 +189,6 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
 struct PsArgs {
   int N = 0, NP = 0, K = 0, E = 0, nt = 0, diag = 0, obs_t0 = 0;
   int s1 = 1, nkb1 = 0, nkb2 = 0, tn = 0;  // tn: column tiles (NP / 32)
-  long long Wp = 0;
   double dt = 0.0;
   const void* Lks[2] = {nullptr, nullptr};  // blocked operands (hi, lo): L_k rows (nrb1 row blocks)
   void* Ls[2] = {nullptr, nullptr};         // Ls, two copies of copy_elems (nrb2 row blocks each)
@@ -409,8 +408,10 @@ __global__ void __cluster_dims__(kPsCluster, 1, 1) __launch_bounds__(kPsThreads,
     for (int q = 0; q < 4; ++q) {
       const int ig = 64 * I + orow + (tid >> 5) + 4 * q, jg = kPsCols * J + ocol;
       if (ig < N && jg < N) {
-        const float2 xt = a.rho[(long long)jg * N + ig];
-        h = fmax(h, hypot((double)rr[q].x - (double)xt.x, (double)rr[q].y + (double)xt.y));
+        // (written by another CTA one grid barrier ago: read past L1)
+        const volatile float* vt = reinterpret_cast<const volatile float*>(a.rho + (long long)jg * N + ig);
+        const float xtx = vt[0], xty = vt[1];
+        h = fmax(h, hypot((double)rr[q].x - (double)xtx, (double)rr[q].y + (double)xty));
         if (ig == jg) {
           tx += rr[q].x;
           ty += rr[q].y;
@@ -741,7 +742,6 @@ int persist_propagate(const GemmRunArgs& a, cudaStream_t st) {
   while (s1 > 1 && (a.Kdense * s1 > kPsCluster || s1 > p.nkb1)) s1 >>= 1;
   p.s1 = s1;
   p.tn = NP / kPsCols;
-  p.Wp = sp.Wp;
   p.dt = a.dt;
   p.nrb1 = a.Kdense * 2 * NP / 64;
   p.nrb2 = 2 * NP / 64;
@@ -773,7 +773,7 @@ int persist_propagate(const GemmRunArgs& a, cudaStream_t st) {
     return LGB_ERR_UNSUPPORTED;
   // the operands (set up and initialised in the K-major arrays) into the
   // blocked layout: L_k once, Ls and Rs into both copies
-  const int cgrid = 8 * 152;
+  const int cgrid = 1024;  // (grid-stride loops)
   if (sp.bf16) {
     if (p.K > 0)
       to_blocks_kernel<true><<<cgrid, 256, 0, st>>>(sp.Lks[0], sp.Lks[1], (long long)p.K * 2 * NP, NP, sp.Lksb[0],
