@@ -501,6 +501,35 @@ def test_gemm_persistent_kernel_vs_oracle(prec, N, K, kind):
     assert np.abs(out[1][0] - out[0][0]).max() < tol
 
 
+def test_gemm_persistent_kernel_sixteen_observables_three_g1_rounds():
+    """The persistent kernel at its limits: 16 observables (every partial
+    slot), K = 9 dense collapse operators (three rounds of G1 products through
+    the one receive buffer), every step stored, against the oracle."""
+    from pyqed_gb300.batch import prepare_batch
+    from pyqed_gb300.engine import Propagator
+    rng = np.random.default_rng(77)
+    N, K, nt, dt = 192, 9, 5, 0.02
+    H, cops, rho0, _ = _random_instance(rng, N, K)
+    eops = [W.gue_matrix(rng, N) for _ in range(16)]
+    obs, states = O.lindblad(H, rho0, cops, eops, Nt=nt, dt=dt)
+    bi = prepare_batch([H], [cops], [rho0], [eops])
+    prop = Propagator(bi.dims, nt=nt, dt=dt, n_cops=bi.n_cops, cops_kind=bi.cops_kind, n_eops=16,
+                      precision="3xtf32", schedule="gemm", store_every=1, obs_t0=True)
+    try:
+        prop.set_operators(bi.H, bi.cops, bi.eops, bi.dops)
+        assert prop.info()["persistent_instances"] == 1
+        o = prop.alloc_outputs(want_obs=True, want_rho=True, want_states=True)
+        prop.propagate_device(prop.to_device(bi.rho0), None, o)
+        prop.check_errors()
+        rho, ob, st = prop.unpack_rho(o[1])[0], prop.unpack_obs(o[0])[0], prop.unpack_states(o[2])[0]
+    finally:
+        prop.close()
+    assert np.abs(rho - states[-1]).max() < TOL32
+    assert np.abs(ob - obs).max() < TOL32 * N
+    for k in range(nt):
+        assert np.abs(st[k] - states[k]).max() < TOL32  # (states[k]: after step k + 1)
+
+
 @pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32", TOL32), ("3xtf32", TOL32)])
 def test_gemm_schedule_graph_replay_vs_oracle(prec, tol):
     """45 steps: two replays of a captured 16-step CUDA graph and one of a
