@@ -212,7 +212,10 @@ int lgb_plan_get_info(lgb_plan_t plan, lgb_plan_info_t* info);
  *                      static instance with 64 < N <= 256 as one persistent
  *                      launch (clusters of 8 CTAs, two grid barriers per RK4
  *                      stage) when the device holds all its CTAs at once;
- *                      0 always uses the graph-replayed kernels
+ *                      0 always uses the graph-replayed kernels (use 0 when
+ *                      other kernels occupy SMs during the propagation: the
+ *                      kernel's grid barriers then give up after 1 s with
+ *                      LGB_ERR_TIMEOUT rather than wait for SMs)
  *   LGB_OPT_CHECK      per-step check of the state, accumulated in FP64:
  *                      0 (default) off; v = 1..15 checks after every step
  *                      that |Tr rho(t) - Tr rho0| <= 10^-v and, for
