@@ -106,19 +106,20 @@ def test_solver_run_check_attribute(golden):
     assert abs(np.trace(states[-1]) - 1.0) < 1e-12
 
 
-@pytest.mark.parametrize("prec", ["3xtf32", "3xbf16"])
-def test_check_on_the_persistent_kernel(prec):
+@pytest.mark.parametrize("prec,nt", [("3xtf32", 40), ("3xbf16", 40), ("3xbf16", 1)])
+def test_check_on_the_persistent_kernel(prec, nt):
     """The persistent split-precision kernel (64 < N <= 256, static) runs the
     per-step check itself: its results are bitwise those of an unchecked
     run, its maxima agree with the graph-replayed kernels' check to
-    rounding, and a tolerance below rounding flags the instance."""
+    rounding, and a tolerance below rounding flags the instance (also for a
+    single step, where only the final step's check runs)."""
     from pyqed_gb300.batch import prepare_batch
     from pyqed_gb300.engine import Propagator
     H, cops, rho0 = _hermitian_batch([200], 2, "dense", seed=7)
     bi = prepare_batch(H, cops, rho0, [[h] for h in H])
     out = {}
     for persist, tol in ((1, None), (1, 1e-3), (0, 1e-3), (1, 1e-15)):
-        prop = Propagator(bi.dims, nt=40, dt=0.02, n_cops=bi.n_cops, cops_kind=bi.cops_kind, n_eops=1,
+        prop = Propagator(bi.dims, nt=nt, dt=0.02, n_cops=bi.n_cops, cops_kind=bi.cops_kind, n_eops=1,
                           precision=prec, schedule="gemm")
         try:
             prop.set_option("gemm_persist", persist)
